@@ -1,0 +1,306 @@
+// capi.cu -- the C ABI of libhydro_gb300.so: the reference's 2D scheme entry
+// points (same signatures and side effects), the native solver API, time-loop
+// planning and error reporting.  Host code only; the kernels live in the
+// per-precision translation units.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "solver2d.h"
+
+// Weak fallback for the caller-defined configuration array: a driver that
+// defines `double config[N_CONF]` (as the reference's drivers do) overrides it.
+extern "C" {
+__attribute__((weak)) double config[N_CONF];
+}
+
+namespace hydro {
+
+static thread_local std::string g_err;
+static std::atomic<unsigned long long> g_launches{0};
+
+void set_error(const std::string& msg) { g_err = msg; }
+void count_launch(unsigned long long k) { g_launches += k; }
+bool cuda_ok(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess)
+        return true;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+RunConfig run_config_from(const double* cfg, int ncfg)
+{
+    auto at = [&](int k) { return k < ncfg ? cfg[k] : INFINITY; };
+    RunConfig r;
+    r.t_all = at(1);
+    r.eps = at(4);
+    r.N = (int)at(5);
+    r.gamma = at(6);
+    r.cfl = at(7);
+    r.hx = at(10);
+    r.hy = at(11);
+    r.cfg16 = at(16);
+    r.bx = (int)at(17);
+    r.by = (int)at(18);
+    r.alpha = at(41);
+    return r;
+}
+
+// Mirrors the control flow of the reference's time loops
+// (grp_solver_2D_EUL_source.c:146-286, grp_solver_2D_split_EUL_source.c:148-337):
+// plot snapshots, the CFL step from the initial data, clipping of the last
+// step to t_all, the tau < eps stop, the non-finite-tau abort and the
+// alternating x-half / y / x-half sweeps of the split scheme.
+RunPlan plan_run(const RunConfig& rc, double hs, int split, const double* time_plot, int N_plot, int N_T)
+{
+    RunPlan P;
+    P.hs_max = hs;
+    int nt = 0, nt_plot = 0, DS = 1, k = 1;
+    double time_c = 0.0, tau = rc.cfg16;
+    double half_tau = 0.0, half_nu = 0.0, nu = 0.0, mu = 0.0;
+    bool stop_after = false;
+    int find_x = 0, find_y = 0;
+    while (k <= rc.N) {
+        int seq_next = (int)P.sweeps.size() + 1;
+        if (time_c >= time_plot[nt_plot] && nt_plot < (N_plot - 1)) {
+            nt_plot++;
+            if (nt < (N_T - 1)) {
+                P.snaps.push_back({seq_next, nt});
+                nt++;
+            }
+        }
+        if (!split || DS) {
+            if (isfinite(rc.t_all) || !isfinite(rc.cfg16) || rc.cfg16 <= 0.0) {
+                tau = rc.cfl * hs;
+                if (tau < rc.eps)
+                    stop_after = true;
+                else if ((time_c + tau) > (rc.t_all - rc.eps))
+                    tau = rc.t_all - time_c;
+                else if (!isfinite(tau))
+                    break;  // abort before the step
+            }
+            if (split) {
+                half_tau = tau * 0.5;
+                half_nu = half_tau / rc.hx;
+                mu = tau / rc.hy;
+            } else {
+                nu = tau / rc.hx;
+                mu = tau / rc.hy;
+            }
+        }
+        if (!split) {
+            SweepRec r{k, 0, tau, nu, mu, find_x, find_y, nt, time_c, 0.0};
+            find_x = find_y = 1;
+            time_c += tau;
+            r.time_after = time_c;
+            P.sweeps.push_back(r);
+            if (stop_after || time_c > (rc.t_all - rc.eps) || !isfinite(time_c))
+                break;
+            ++k;
+        } else {
+            SweepRec rx{k, 1, half_tau, half_nu, 0.0, find_x, find_y, nt, time_c, time_c};
+            find_x = 1;
+            P.sweeps.push_back(rx);
+            if (stop_after)
+                break;
+            if (DS) {
+                SweepRec ry{k, 2, tau, 0.0, mu, find_x, find_y, nt, time_c, time_c + tau};
+                find_y = 1;
+                time_c += tau;
+                ry.time_after = time_c;
+                P.sweeps.push_back(ry);
+            }
+            if (stop_after || time_c > (rc.t_all - rc.eps) || !isfinite(time_c))
+                break;
+            DS = DS ? 0 : 1;
+            if (!DS)
+                ++k;
+        }
+    }
+    P.end_k = k;
+    P.end_time = time_c;
+    P.end_tau = tau;
+    P.end_nt = nt;
+    return P;
+}
+
+static int form_from_config(const double* cfg)
+{
+    double f = cfg[300];
+    if (!isfinite(f))
+        return HYDRO_FORM_FP64;
+    return (int)f;
+}
+
+static Solver2DBase* make_solver(int m, int n, int form)
+{
+    switch (form) {
+    case HYDRO_FORM_FP64:
+        return make_solver2d_f64(m, n);
+    case HYDRO_FORM_FP32:
+        return make_solver2d_f32(m, n, 0);
+    case HYDRO_FORM_FP32_LEARNED:
+        return make_solver2d_f32(m, n, 1);
+    default:
+        set_error("unknown form");
+        return nullptr;
+    }
+}
+
+// Shared body of the two 2D scheme entry points.
+static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, double* cpu_time, int N_T, int* N_plot,
+                         double time_plot[], int split)
+{
+    const double t_all = config[1];
+    const int form = form_from_config(config);
+    Solver2DBase* s = make_solver(m, n, form);
+    if (!s) {
+        fprintf(stderr, "hydro_gb300: cannot create the 2D solver: %s\n", hydro_gb300_last_error());
+        exit(5);
+    }
+    size_t mn = (size_t)m * n;
+    std::vector<double> host(5 * mn);
+    double* pl[5] = {&host[0], &host[mn], &host[2 * mn], &host[3 * mn], &host[4 * mn]};
+    for (int j = 0; j < m; ++j) {
+        memcpy(pl[0] + (size_t)j * n, CV[0].RHO[j], n * sizeof(double));
+        memcpy(pl[1] + (size_t)j * n, CV[0].U[j], n * sizeof(double));
+        memcpy(pl[2] + (size_t)j * n, CV[0].V[j], n * sizeof(double));
+        memcpy(pl[3] + (size_t)j * n, CV[0].P[j], n * sizeof(double));
+        memcpy(pl[4] + (size_t)j * n, CV[0].E[j], n * sizeof(double));
+    }
+    if (s->upload(pl[0], pl[1], pl[2], pl[3], pl[4], config[6])) {
+        fprintf(stderr, "hydro_gb300: upload failed: %s\n", hydro_gb300_last_error());
+        exit(5);
+    }
+    std::vector<std::vector<double>> snaps(N_T);
+    std::vector<double*> snap_ptr(N_T, nullptr);
+    for (int k = 1; k < N_T - 1; ++k) {  // CV[0] keeps the initial data, no copy needed
+        snaps[k].resize(5 * mn);
+        snap_ptr[k] = snaps[k].data();
+    }
+    RunConfig rc = run_config_from(config, N_CONF);
+    hydro_run_info info;
+    int nt = 0;
+    if (s->run(rc, split, 0, time_plot, *N_plot, N_T, snap_ptr.data(), &info, &nt)) {
+        fprintf(stderr, "hydro_gb300: time loop failed: %s\n", hydro_gb300_last_error());
+        exit(5);
+    }
+    if (s->download(pl[0], pl[1], pl[2], pl[3], pl[4])) {
+        fprintf(stderr, "hydro_gb300: download failed: %s\n", hydro_gb300_last_error());
+        exit(5);
+    }
+    delete s;
+    auto scatter = [&](int k, const double* src) {
+        for (int j = 0; j < m; ++j) {
+            memcpy(CV[k].RHO[j], src + (size_t)j * n, n * sizeof(double));
+            memcpy(CV[k].U[j], src + mn + (size_t)j * n, n * sizeof(double));
+            memcpy(CV[k].V[j], src + 2 * mn + (size_t)j * n, n * sizeof(double));
+            memcpy(CV[k].P[j], src + 3 * mn + (size_t)j * n, n * sizeof(double));
+            memcpy(CV[k].E[j], src + 4 * mn + (size_t)j * n, n * sizeof(double));
+        }
+    };
+    for (int k = 1; k < nt; ++k)  // CV[0] already holds the initial data
+        scatter(k, snaps[k].data());
+    scatter(nt, host.data());
+
+    if (info.halted == 1)
+        printf("Error on the time step %d (x-face code %d, y-face code %d); the step was discarded.\n", info.k_out,
+               info.error_code_x, info.error_code_y);
+    else if (info.halted == 2)
+        printf("Error on the time step %d (x-face code %d, y-face code %d, or a non-positive update); stopped after the step.\n",
+               info.k_out, info.error_code_x, info.error_code_y);
+    printf("\nTime is up at time step %d.\n", info.k_out);
+    printf("The cost of GPU time for the %s 2D-GRP Eulerian scheme for this problem is %g seconds.\n",
+           split ? "dimension-split" : "unsplit", info.gpu_ms * 1e-3);
+    config[5] = (double)info.k_out;
+    *N_plot = nt + 1;
+    if (isfinite(info.time))
+        time_plot[nt] = info.time;
+    else if (isfinite(t_all))
+        time_plot[nt] = t_all;
+    else if (isfinite(info.tau))
+        time_plot[nt] = info.k_out * info.tau;
+    for (int k = 0; k <= nt; ++k)
+        cpu_time[k] = info.gpu_ms * 1e-3;
+}
+
+}  // namespace hydro
+
+using namespace hydro;
+
+struct hydro2d {
+    Solver2DBase* s;
+};
+
+extern "C" {
+
+const char* hydro_gb300_last_error(void) { return g_err.c_str(); }
+unsigned long long hydro_gb300_kernel_launches(void) { return g_launches.load(); }
+
+int hydro2d_create(hydro2d_t** out, int m, int n, int form)
+{
+    *out = nullptr;
+    if (m < 2 || n < 2) {
+        set_error("grid must be at least 2 x 2");
+        return -1;
+    }
+    Solver2DBase* s = make_solver(m, n, form);
+    if (!s)
+        return -1;
+    *out = new hydro2d{s};
+    return 0;
+}
+
+void hydro2d_destroy(hydro2d_t* h)
+{
+    if (!h)
+        return;
+    delete h->s;
+    delete h;
+}
+
+int hydro2d_upload(hydro2d_t* h, const double* rho, const double* u, const double* v, const double* p, const double* E,
+                   double gamma)
+{
+    return h->s->upload(rho, u, v, p, E, gamma);
+}
+
+int hydro2d_download(hydro2d_t* h, double* rho, double* u, double* v, double* p, double* E)
+{
+    return h->s->download(rho, u, v, p, E);
+}
+
+int hydro2d_run(hydro2d_t* h, const double* cfg, int ncfg, int split, int stats, hydro_run_info* info)
+{
+    RunConfig rc = run_config_from(cfg, ncfg);
+    double tp[2] = {0.0, rc.t_all};
+    int nt = 0;
+    return h->s->run(rc, split, stats, tp, 2, 2, nullptr, info, &nt);
+}
+
+void GRP_solver_2D_EUL_source(const int m, const int n, struct cell_var_stru* CV, double** X, double** Y,
+                              double* cpu_time, const char* problem, int N_T, int* N_plot, double time_plot[])
+{
+    (void)X;
+    (void)Y;
+    (void)problem;
+    run_2d_entry(m, n, CV, cpu_time, N_T, N_plot, time_plot, 0);
+}
+
+void GRP_solver_2D_split_EUL_source(const int m, const int n, struct cell_var_stru* CV, double** X, double** Y,
+                                    double* cpu_time, const char* problem, int N_T, int* N_plot, double time_plot[])
+{
+    (void)X;
+    (void)Y;
+    (void)problem;
+    run_2d_entry(m, n, CV, cpu_time, N_T, N_plot, time_plot, 1);
+}
+
+}  // extern "C"

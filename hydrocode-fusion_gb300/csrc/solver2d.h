@@ -1,0 +1,74 @@
+// solver2d.h -- host-side interface shared by the 2D solver translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <string>
+#include <vector>
+
+#include "../../include/hydro_gb300.h"
+
+namespace hydro {
+
+// Run configuration taken from config[] (indices of the reference's doc/config.csv).
+struct RunConfig {
+    double t_all, eps, gamma, cfl, hx, hy, cfg16, alpha;
+    int N, bx, by;
+};
+RunConfig run_config_from(const double* cfg, int ncfg);
+
+// A plot snapshot request: before which launch the current state is recorded.
+struct SnapshotPlan {
+    int seq;  // record the state just before launch `seq` (1-based)
+    int nt;   // snapshot index it becomes (CV[nt])
+};
+
+// The host-side plan of a time loop: one record per kernel launch, computed
+// with the same double arithmetic as the reference's loop.
+struct SweepRec {
+    int k;             // reference step counter during this launch
+    int dir;           // 0 unsplit step, 1 x-sweep, 2 y-sweep
+    double tau_face;   // time step passed to the GRP flux
+    double fac_x, fac_y;  // nu (tau/h_x, or half_tau/h_x) and mu
+    int find_x, find_y;
+    int nt;            // snapshot index the state lives in during this launch
+    double time_before, time_after;
+};
+
+struct RunPlan {
+    std::vector<SweepRec> sweeps;
+    std::vector<SnapshotPlan> snaps;
+    int end_k;           // config[5] if nothing halts on the device
+    double end_time;     // time_c at the end of the plan
+    double end_tau;
+    int end_nt;
+    double hs_max;       // CFL h/S_max from the initial data
+};
+
+// Builds the plan. time_plot: plot times (time_plot[0] = 0, last = t_all), N_T
+// stored snapshots at most.
+RunPlan plan_run(const RunConfig& rc, double h_S_max, int split, const double* time_plot, int N_plot, int N_T);
+
+// Type-erased solver (FP64 and FP32 instantiations live in separate TUs).
+class Solver2DBase {
+public:
+    virtual ~Solver2DBase() {}
+    virtual int upload(const double* rho, const double* u, const double* v, const double* p, const double* E,
+                       double gamma) = 0;
+    virtual int download(double* rho, double* u, double* v, double* p, double* E) = 0;
+    // Runs the plan; snapshots (if any) are written as 5 x-major planes
+    // (rho,u,v,p,E) each into snap_out[nt] (host memory, may be null).
+    virtual int run(const RunConfig& rc, int split, int stats, const double* time_plot, int N_plot, int N_T,
+                    double** snap_out, hydro_run_info* info, int* final_nt) = 0;
+    int m = 0, n = 0, form = 0;
+};
+
+Solver2DBase* make_solver2d_f64(int m, int n);
+Solver2DBase* make_solver2d_f32(int m, int n, int learned);
+
+// error reporting + launch counting shared by all TUs
+void set_error(const std::string& msg);
+void count_launch(unsigned long long k = 1);
+bool cuda_ok(cudaError_t e, const char* what);
+
+}  // namespace hydro

@@ -1,0 +1,19 @@
+// solver2d_f64.cu -- FP64 (parity) instantiation of the 2D solver.
+// Compiled with --fmad=false: no multiply-add contraction, IEEE division and
+// square root, so every operation rounds exactly as the reference's C code
+// (only pow() differs from glibc's, by at most a couple of ulp).
+#include "solver2d_impl.cuh"
+
+namespace hydro {
+
+Solver2DBase* make_solver2d_f64(int m, int n)
+{
+    Solver2D<double>* s = new Solver2D<double>();
+    if (s->init(m, n, HYDRO_FORM_FP64)) {
+        delete s;
+        return nullptr;
+    }
+    return s;
+}
+
+}  // namespace hydro

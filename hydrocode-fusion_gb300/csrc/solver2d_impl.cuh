@@ -1,0 +1,452 @@
+// solver2d_impl.cuh -- host side of the 2D solver, instantiated per precision.
+//
+// Memory: one cudaMalloc per solver holding 26 planes of m x ld elements
+// (two 13-plane states: rho,u,v,p,E + 4 x-slopes + 4 y-slopes), plus the -1
+// boundary table and the control block.  ld is n rounded up to 32 elements so
+// every x-station starts on a 128-byte boundary.  At 4096^2 that is 3.5 GB in
+// FP64 and 1.75 GB in FP32: far below HBM capacity, so nothing is ever paged.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "solver2d.h"
+#include "step2d.cuh"
+
+namespace hydro {
+
+// Tile shapes of the fused kernels.
+template <typename R> struct Tiles;
+template <> struct Tiles<double> {
+    static constexpr int TJ = 16, TI = 16, NT = 256;       // unsplit step
+    static constexpr int SJ = 16, SI = 32, SNT = 256;      // split sweeps
+};
+template <> struct Tiles<float> {
+    static constexpr int TJ = 16, TI = 32, NT = 512;
+    static constexpr int SJ = 16, SI = 32, SNT = 256;
+};
+
+// ---------------------------------------------------------------------------
+// helper kernels
+// ---------------------------------------------------------------------------
+
+// Copy an x-major FP64 host-layout plane (staged on the device) into a pitched plane.
+template <typename R>
+__global__ void k_pack_plane(const double* __restrict__ in, R* __restrict__ out, int m, int n, int ld)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t total = (size_t)m * n;
+    for (; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(idx / n), i = (int)(idx - (size_t)j * n);
+        out[(size_t)j * ld + i] = (R)in[idx];
+    }
+}
+
+template <typename R>
+__global__ void k_unpack_plane(const R* __restrict__ in, double* __restrict__ out, int m, int n, int ld)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t total = (size_t)m * n;
+    for (; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(idx / n), i = (int)(idx - (size_t)j * n);
+        out[idx] = (double)in[(size_t)j * ld + i];
+    }
+}
+
+// E = 0.5 u^2 + p/(gamma-1)/rho; E += 0.5 v^2 (the driver's formula,
+// src/hydrocode_2D/hydrocode.c:252-253), evaluated in FP64.
+static __global__ void k_energy(const double* rho, const double* u, const double* v, const double* p, double* E, size_t total,
+                         double gamma)
+{
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        double e = 0.5 * u[idx] * u[idx] + p[idx] / (gamma - 1.0) / rho[idx];
+        e += 0.5 * v[idx] * v[idx];
+        E[idx] = e;
+    }
+}
+
+// Edge values of the initial state for the fixed (-1) boundary code:
+// [4][n] left (j=0), [4][n] right (j=m-1), [4][m] down (i=0), [4][m] up (i=n-1).
+template <typename R>
+__global__ void k_ghost0(const R* __restrict__ w, size_t plane, int m, int n, int ld, R* __restrict__ g)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        for (int k = 0; k < 4; ++k) {
+            g[k * n + t] = w[k * plane + t];
+            g[4 * n + k * n + t] = w[k * plane + (size_t)(m - 1) * ld + t];
+        }
+    }
+    if (t < m) {
+        for (int k = 0; k < 4; ++k) {
+            g[8 * n + k * m + t] = w[k * plane + (size_t)t * ld];
+            g[8 * n + 4 * m + k * m + t] = w[k * plane + (size_t)t * ld + (n - 1)];
+        }
+    }
+}
+
+// CFL: h_S_max = min over cells of min(h_x,h_y)/(|c|+|u|+|v|), c = sqrt(gamma p/rho),
+// in FP64 (grp_solver_2D_EUL_source.c:180-188).  fmin is exact, so the
+// warp-shuffle/atomic reduction order cannot change the result.  The minimum
+// of non-negative doubles is taken on their bit patterns (same order).
+template <typename R>
+__global__ void k_cfl_min(const R* __restrict__ w, size_t plane, int m, int n, int ld, double gamma, double hmin,
+                          unsigned long long* __restrict__ out)
+{
+    double best = INFINITY;
+    size_t total = (size_t)m * n;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(idx / n), i = (int)(idx - (size_t)j * n);
+        size_t o = (size_t)j * ld + i;
+        double rho = (double)w[o], u = (double)w[plane + o], v = (double)w[2 * plane + o], p = (double)w[3 * plane + o];
+        double c = sqrt(gamma * p / rho);
+        double sigma = fabs(c) + fabs(u) + fabs(v);
+        best = fmin(best, hmin / sigma);
+    }
+    for (int off = 16; off; off >>= 1)
+        best = fmin(best, __shfl_xor_sync(0xffffffffu, best, off));
+    __shared__ double red[32];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+        red[wid] = best;
+    __syncthreads();
+    if (wid == 0) {
+        best = (lane < (int)(blockDim.x >> 5)) ? red[lane] : INFINITY;
+        for (int off = 16; off; off >>= 1)
+            best = fmin(best, __shfl_xor_sync(0xffffffffu, best, off));
+        if (lane == 0 && !(best != best))
+            atomicMin(out, (unsigned long long)__double_as_longlong(best));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the solver
+// ---------------------------------------------------------------------------
+template <typename R>
+class Solver2D : public Solver2DBase {
+public:
+    int ld = 0;
+    size_t plane = 0;
+    R* mem = nullptr;
+    R* ghost0 = nullptr;
+    Ctl* ctl = nullptr;
+    double* stage = nullptr;   // FP64 staging, 5 planes of m*n
+    unsigned long long* red = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int sms = 148;
+
+    R* W(int b) { return mem + (size_t)b * 13 * plane; }
+    R* Sx(int b) { return W(b) + 5 * plane; }
+    R* Ty(int b) { return W(b) + 9 * plane; }
+
+    int init(int m_, int n_, int form_)
+    {
+        m = m_;
+        n = n_;
+        form = form_;
+        ld = (n + 31) / 32 * 32;
+        plane = (size_t)m * ld;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (!cuda_ok(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream")) return -1;
+        if (!cuda_ok(cudaEventCreate(&ev0), "event")) return -1;
+        if (!cuda_ok(cudaEventCreate(&ev1), "event")) return -1;
+        if (!cuda_ok(cudaMalloc(&mem, sizeof(R) * 26 * plane), "state buffers")) return -1;
+        if (!cuda_ok(cudaMemset(mem, 0, sizeof(R) * 26 * plane), "state clear")) return -1;
+        if (!cuda_ok(cudaMalloc(&ghost0, sizeof(R) * (8 * (size_t)n + 8 * (size_t)m)), "ghost table")) return -1;
+        if (!cuda_ok(cudaMalloc(&ctl, sizeof(Ctl)), "control block")) return -1;
+        if (!cuda_ok(cudaMalloc(&stage, sizeof(double) * 5 * (size_t)m * n), "staging")) return -1;
+        if (!cuda_ok(cudaMalloc(&red, sizeof(unsigned long long)), "reduction")) return -1;
+        using TS = Tiles<R>;
+        size_t smem_u = UnsplitSmem<R, TS::TJ, TS::TI>::bytes;
+        size_t smem_x = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SJ, TS::SI);
+        size_t smem_y = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SI, TS::SJ);
+        if (!cuda_ok(cudaFuncSetAttribute(k_step_unsplit<R, TS::TJ, TS::TI, TS::NT>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u), "smem attr"))
+            return -1;
+        if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x), "smem attr"))
+            return -1;
+        if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y), "smem attr"))
+            return -1;
+        return 0;
+    }
+
+    ~Solver2D() override
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        cudaFree(mem);
+        cudaFree(ghost0);
+        cudaFree(ctl);
+        cudaFree(stage);
+        cudaFree(red);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int grid1d(size_t total) const
+    {
+        size_t b = (total + 255) / 256;
+        size_t cap = (size_t)sms * 8;
+        return (int)(b < cap ? (b ? b : 1) : cap);
+    }
+
+    int upload(const double* rho, const double* u, const double* v, const double* p, const double* E,
+               double gamma) override
+    {
+        size_t mn = (size_t)m * n;
+        const double* src[4] = {rho, u, v, p};
+        for (int k = 0; k < 4; ++k)
+            if (!cuda_ok(cudaMemcpyAsync(stage + k * mn, src[k], sizeof(double) * mn, cudaMemcpyHostToDevice, stream),
+                         "upload"))
+                return -1;
+        if (E) {
+            if (!cuda_ok(cudaMemcpyAsync(stage + 4 * mn, E, sizeof(double) * mn, cudaMemcpyHostToDevice, stream), "upload"))
+                return -1;
+        } else {
+            k_energy<<<grid1d(mn), 256, 0, stream>>>(stage, stage + mn, stage + 2 * mn, stage + 3 * mn, stage + 4 * mn,
+                                                       mn, gamma);
+            count_launch();
+        }
+        for (int k = 0; k < 5; ++k) {
+            k_pack_plane<R><<<grid1d(mn), 256, 0, stream>>>(stage + k * mn, W(0) + k * plane, m, n, ld);
+            count_launch();
+        }
+        // slopes start at zero (the first limiting uses minmod2 and ignores them)
+        if (!cuda_ok(cudaMemsetAsync(Sx(0), 0, sizeof(R) * 8 * plane, stream), "clear")) return -1;
+        if (!cuda_ok(cudaMemsetAsync(Sx(1), 0, sizeof(R) * 8 * plane, stream), "clear")) return -1;
+        cur_w = cur_s = cur_t = 0;
+        return cuda_ok(cudaStreamSynchronize(stream), "upload sync") ? 0 : -1;
+    }
+
+    int download_planes(int b, double* const dst[5])
+    {
+        size_t mn = (size_t)m * n;
+        for (int k = 0; k < 5; ++k) {
+            if (!dst[k])
+                continue;
+            k_unpack_plane<R><<<grid1d(mn), 256, 0, stream>>>(W(b) + k * plane, stage + k * mn, m, n, ld);
+            count_launch();
+            if (!cuda_ok(cudaMemcpyAsync(dst[k], stage + k * mn, sizeof(double) * mn, cudaMemcpyDeviceToHost, stream),
+                         "download"))
+                return -1;
+        }
+        return cuda_ok(cudaStreamSynchronize(stream), "download sync") ? 0 : -1;
+    }
+
+    int download(double* rho, double* u, double* v, double* p, double* E) override
+    {
+        double* dst[5] = {rho, u, v, p, E};
+        return download_planes(cur_w, dst);
+    }
+
+    double cfl_hsmax(double gamma, double hmin)
+    {
+        unsigned long long init = 0x7ff0000000000000ull;  // +inf
+        cudaMemcpyAsync(red, &init, sizeof(init), cudaMemcpyHostToDevice, stream);
+        k_cfl_min<R><<<grid1d((size_t)m * n), 256, 0, stream>>>(W(cur_w), plane, m, n, ld, gamma, hmin, red);
+        count_launch();
+        unsigned long long bits = 0;
+        cudaMemcpyAsync(&bits, red, sizeof(bits), cudaMemcpyDeviceToHost, stream);
+        cudaStreamSynchronize(stream);
+        double r;
+        memcpy(&r, &bits, sizeof(r));
+        return r;
+    }
+
+    int cur_w = 0, cur_s = 0, cur_t = 0;
+
+    void fill_gas(Gas<R>& G, double g, double eps)
+    {
+        double zeta = (g - 1.0) / (g + 1.0);
+        G.g = (R)g;
+        G.gm1 = (R)(g - 1.0);
+        G.zeta = (R)zeta;
+        G.mu = (R)((g - 1.0) / (2.0 * g));
+        G.nu = (R)((g + 1.0) / (2.0 * g));
+        G.g_g1 = (R)(g / (g - 1.0));
+        G.inv_g = (R)(1.0 / g);
+        G.cexp = (R)(0.5 * (g - 1.0) / g);
+        G.sexp = (R)(2.0 * g / (g - 1.0));
+        G.e1 = (R)(0.5 / zeta);
+        G.e2 = (R)((1.0 + zeta) / zeta);
+        G.opz = (R)(1.0 + zeta);
+        G.op2z = (R)(1.0 + 2.0 * zeta);
+        G.eps = (R)eps;
+        G.g64 = g;
+        G.eps64 = eps;
+    }
+
+    static bool is_pow2(double h)
+    {
+        int e;
+        double f = frexp(h, &e);
+        return h > 0.0 && f == 0.5;
+    }
+
+    int run(const RunConfig& rc, int split, int stats, const double* time_plot, int N_plot, int N_T,
+            double** snap_out, hydro_run_info* info, int* final_nt) override
+    {
+        memset(info, 0, sizeof(*info));
+        // ghost table for the fixed boundary, from the initial state
+        {
+            int t = (m > n ? m : n);
+            k_ghost0<R><<<(t + 255) / 256, 256, 0, stream>>>(W(cur_w), plane, m, n, ld, ghost0);
+            count_launch();
+        }
+        double hs = cfl_hsmax(rc.gamma, fmin(rc.hx, rc.hy));
+        RunPlan plan = plan_run(rc, hs, split, time_plot, N_plot, N_T);
+        if (!cuda_ok(cudaMemsetAsync(ctl, 0, sizeof(Ctl), stream), "ctl clear")) return -1;
+
+        StepArgs<R> a;
+        memset(&a, 0, sizeof(a));
+        a.m = m;
+        a.n = n;
+        a.ld = ld;
+        a.plane = plane;
+        a.ghost0 = ghost0;
+        fill_gas(a.G, rc.gamma, rc.eps);
+        a.hx = (R)rc.hx;
+        a.hy = (R)rc.hy;
+        a.hhx = (R)(0.5 * rc.hx);
+        a.hhy = (R)(0.5 * rc.hy);
+        a.pow2_x = is_pow2(rc.hx);
+        a.pow2_y = is_pow2(rc.hy);
+        a.inv_hx = (R)(1.0 / rc.hx);
+        a.inv_hy = (R)(1.0 / rc.hy);
+        a.alpha = (R)rc.alpha;
+        a.bx = rc.bx;
+        a.by = rc.by;
+        a.ctl = ctl;
+        a.stats = stats;
+
+        using TS = Tiles<R>;
+        dim3 gu((n + TS::TI - 1) / TS::TI, (m + TS::TJ - 1) / TS::TJ);
+        dim3 gs((n + TS::SI - 1) / TS::SI, (m + TS::SJ - 1) / TS::SJ);
+        size_t smem_u = UnsplitSmem<R, TS::TJ, TS::TI>::bytes;
+        size_t smem_x = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SJ, TS::SI);
+        size_t smem_y = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SI, TS::SJ);
+
+        // snapshots: pinned staging per requested snapshot
+        std::vector<double*> snap_dev;
+        size_t mn = (size_t)m * n;
+        size_t snap_next = 0;
+        int wbuf_at_seq0 = cur_w;
+        std::vector<int> wbuf_before(plan.sweeps.size() + 1);
+
+        cudaEventRecord(ev0, stream);
+        int w = cur_w, s = cur_s, t = cur_t;
+        for (size_t q = 0; q < plan.sweeps.size(); ++q) {
+            const SweepRec& r = plan.sweeps[q];
+            int seq = (int)q + 1;
+            while (snap_next < plan.snaps.size() && plan.snaps[snap_next].seq == seq) {
+                // record the state in front of this launch
+                if (snap_out && snap_out[plan.snaps[snap_next].nt]) {
+                    double* dst[5];
+                    for (int k = 0; k < 5; ++k)
+                        dst[k] = snap_out[plan.snaps[snap_next].nt] + k * mn;
+                    // ordered on the stream: the state is exactly the one before launch seq
+                    if (download_planes(w, dst)) return -1;
+                }
+                snap_next++;
+            }
+            wbuf_before[q] = w;
+            a.seq = seq;
+            a.find_x = r.find_x;
+            a.find_y = r.find_y;
+            a.tau = (R)r.tau_face;
+            a.htau = (R)(0.5 * r.tau_face);
+            a.nu = (R)r.fac_x;
+            a.mu = (R)r.fac_y;
+            a.src_w = W(w);
+            a.dst_w = W(w ^ 1);
+            if (r.dir == 0) {
+                a.src_s = Sx(s); a.dst_s = Sx(s ^ 1);
+                a.src_t = Ty(t); a.dst_t = Ty(t ^ 1);
+                k_step_unsplit<R, TS::TJ, TS::TI, TS::NT><<<gu, TS::NT, smem_u, stream>>>(a);
+                s ^= 1;
+                t ^= 1;
+            } else if (r.dir == 1) {
+                a.src_s = Sx(s); a.dst_s = Sx(s ^ 1);
+                a.src_t = Ty(t); a.dst_t = Ty(t);
+                k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT><<<gs, TS::SNT, smem_x, stream>>>(a);
+                s ^= 1;
+            } else {
+                a.src_s = Sx(s); a.dst_s = Sx(s);
+                a.src_t = Ty(t); a.dst_t = Ty(t ^ 1);
+                k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT><<<gs, TS::SNT, smem_y, stream>>>(a);
+                t ^= 1;
+            }
+            count_launch();
+            w ^= 1;
+            if (!cuda_ok(cudaGetLastError(), "step launch")) return -1;
+        }
+        wbuf_before[plan.sweeps.size()] = w;
+        cudaEventRecord(ev1, stream);
+        Ctl hc;
+        if (!cuda_ok(cudaMemcpyAsync(&hc, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, stream), "ctl read")) return -1;
+        if (!cuda_ok(cudaStreamSynchronize(stream), "time loop")) return -1;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        (void)wbuf_at_seq0;
+
+        // resolve the outcome
+        int nsw = (int)plan.sweeps.size();
+        int halt_q = 0, kind = 0;  // 1-based launch that halted the run
+        if (hc.halted_seq) {
+            halt_q = hc.halted_seq;
+            kind = hc.halt_kind;
+        } else if (nsw > 0) {
+            int ls = nsw % 3;
+            int d = halt_decision(hc.key[ls][0], hc.key[ls][1], hc.upd_bad[ls]);
+            if (d) {
+                halt_q = nsw;
+                kind = d;
+            }
+        }
+        int final_w;
+        if (halt_q) {
+            const SweepRec& r = plan.sweeps[halt_q - 1];
+            int hs3 = halt_q % 3;
+            info->error_code_x = (int)(hc.key[hs3][0] & 3ull);
+            info->error_code_y = (int)(hc.key[hs3][1] & 3ull);
+            info->halted = kind;
+            info->k_out = r.k;
+            info->time = (kind == 1) ? r.time_before : r.time_after;
+            info->tau = r.tau_face;
+            final_w = (kind == 1) ? wbuf_before[halt_q - 1] : wbuf_before[halt_q];
+            *final_nt = r.nt;
+            info->sweeps_launched = nsw;
+            int kept = (kind == 1) ? halt_q - 1 : halt_q;
+            info->steps_done = kept;
+        } else {
+            info->k_out = plan.end_k;
+            info->time = plan.end_time;
+            info->tau = plan.end_tau;
+            final_w = wbuf_before[nsw];
+            *final_nt = plan.end_nt;
+            info->sweeps_launched = nsw;
+            info->steps_done = nsw;
+        }
+        info->gpu_ms = ms;
+        info->newton_faces = hc.newton_faces;
+        info->newton_iters = hc.newton_iters;
+        cur_w = final_w;
+        // slopes are scratch after the run (the reference frees them)
+        cur_s = s;
+        cur_t = t;
+        return 0;
+    }
+};
+
+}  // namespace hydro

@@ -1,0 +1,647 @@
+// step2d.cuh -- fused 2D GRP time-step kernels (one launch per step/sweep).
+//
+// Device layout (every field a plane, x-major like the reference's CV.X[j][i]):
+//   value of cell (x = j, y = i) at plane[j*ld + i], 0 <= j < m, 0 <= i < n,
+//   so y is the contiguous axis.  A state is 13 planes: rho, u, v, p, E, the
+//   four x-slopes s_* and the four y-slopes t_* (the slopes are genuine state:
+//   the next step's minmod3 limiter uses them).
+//
+// One CTA owns a TJ x TI tile of cells and, in one launch:
+//   1. stages rho,u,v,p of the tile plus a 2-cell halo in shared memory,
+//      applying the boundary condition to ghost cells
+//      (bound_cond_slope_limiter_x.c:34-82, _y.c:34-82);
+//   2. limits the x- and y-slopes of the tile plus a 1-cell halo
+//      (minmod_limiter_2D_x, slope_limiter_2D_x.c:32-84; minmod_limiter,
+//      slope_limiter.c:31-83) and sets the ghost slopes by the boundary rules
+//      (bound_cond_slope_limiter_x.c:94-126, _y.c:94-126);
+//   3. solves every x- and y-face of the tile once (flux_generator_x.c:40-163,
+//      flux_generator_y.c:40-163, GRP_2D_flux) into shared memory;
+//   4. updates the cells and writes the new slopes from the t+tau interface
+//      values (grp_solver_2D_EUL_source.c:228-263).
+// Halo cells are recomputed by the neighbouring CTAs; nothing is written in
+// place, the state ping-pongs between two buffers.
+//
+// Errors never trap: each face's code (ifvar_check -> 1, star/derivative
+// check -> 2) is folded into a 64-bit key (serial index of the face in the
+// reference's loop order, code) with atomicMax, so the host sees exactly the
+// code the reference's serial loop would return (the last failing face
+// wins).  The next launch reads the previous launch's keys and stops the run
+// the way the reference does (abort = discard the step, stop = keep it).
+#pragma once
+
+#include "hydro_device.cuh"
+
+namespace hydro {
+
+// Error/halt control block, one per solver, in device memory.
+struct Ctl {
+    unsigned long long key[3][2];  // [slot][0 = x-faces, 1 = y-faces]
+    unsigned int upd_bad[3];       // positivity failure of the update
+    int halted_seq;                // sequence number of the launch whose flags halted the run (0 = none)
+    int halt_kind;                 // 1 = abort (that launch is discarded), 2 = stop (kept)
+    unsigned long long newton_faces;  // faces that ran the exact solver
+    unsigned long long newton_iters;  // Newton iterations summed over those faces
+    unsigned long long pad[4];
+};
+
+template <typename R>
+struct StepArgs {
+    int m, n, ld;
+    size_t plane;          // elements per plane
+    const R* src_w;        // 5 planes: rho u v p E (input state)
+    R* dst_w;              // 5 planes (output state)
+    const R* src_s;        // 4 planes x-slopes (previous step's)
+    R* dst_s;
+    const R* src_t;        // 4 planes y-slopes
+    R* dst_t;
+    const R* ghost0;       // boundary code -1: initial edge values [4][n] left, [4][n] right, [4][m] down, [4][m] up
+    Gas<R> G;
+    R tau, htau;           // face time step and its half
+    R hx, hy, hhx, hhy;    // grid sizes and their halves
+    R inv_hx, inv_hy;      // exact reciprocals (used only when the size is a power of two)
+    int pow2_x, pow2_y;
+    R nu, mu;              // tau/h_x and tau/h_y of the update
+    R alpha;               // minmod parameter
+    int bx, by;            // boundary codes
+    int find_x, find_y;    // 0 on the first limiting of that direction (minmod2), then 1 (minmod3)
+    Ctl* ctl;
+    int seq;               // launch sequence number (1, 2, ...) of this sweep
+    int split_kind;        // 0 unsplit; for split sweeps the direction is the template parameter
+    int stats;             // count Newton faces / iterations
+};
+
+// ---------------------------------------------------------------------------
+// halting protocol
+// ---------------------------------------------------------------------------
+
+// Decision from a finished launch's flags: 0 continue, 1 abort, 2 stop.
+__device__ __host__ inline int halt_decision(unsigned long long kx, unsigned long long ky, unsigned int ub)
+{
+    int cx = (int)(kx & 3ull), cy = (int)(ky & 3ull);
+    if (cx == 1 || cy == 1)
+        return 1;
+    if (cx == 2 || cy == 2 || ub)
+        return 2;
+    return 0;
+}
+
+// Returns true if this launch must not run.  Thread (0,0) of block (0,0) also
+// records the halt and clears the slot the next launch will write.
+__device__ __forceinline__ bool halt_prologue(Ctl* ctl, int seq)
+{
+    volatile Ctl* c = ctl;
+    bool first = (threadIdx.x == 0 && threadIdx.y == 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0);
+    if (c->halted_seq)
+        return true;
+    if (seq > 1) {
+        int ps = (seq - 1) % 3;
+        int d = halt_decision(c->key[ps][0], c->key[ps][1], c->upd_bad[ps]);
+        if (d) {
+            if (first) {
+                c->halt_kind = d;
+                c->halted_seq = seq - 1;
+            }
+            return true;
+        }
+    }
+    if (first) {
+        int ns = (seq + 1) % 3;
+        c->key[ns][0] = 0ull;
+        c->key[ns][1] = 0ull;
+        c->upd_bad[ns] = 0u;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// boundary-aware load of rho,u,v,p of cell (j, i), possibly a ghost
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void load_prims(const StepArgs<R>& a, int j, int i, R w[4])
+{
+    const int m = a.m, n = a.n;
+    bool outx = (j < 0 || j >= m), outy = (i < 0 || i >= n);
+    int jj = j, ii = i;
+    R su = R(1), sv = R(1);
+    int g0 = -1;  // index into the -1 (initial value) ghost table
+    if (outx) {
+        if (a.bx == -7) {
+            jj = j < 0 ? j + m : j - m;
+        } else {
+            jj = j < 0 ? 0 : m - 1;
+            if (a.bx == -2 || (a.bx == -24 && j < 0))
+                su = R(-1);
+            if (a.bx == -1 && !outy)
+                g0 = (j < 0 ? 0 : 4 * n) + i;  // left table, right table
+        }
+    }
+    if (outy) {
+        if (a.by == -7) {
+            ii = i < 0 ? i + n : i - n;
+        } else {
+            ii = i < 0 ? 0 : n - 1;
+            if (a.by == -2 || (a.by == -24 && i < 0))
+                sv = R(-1);
+            if (a.by == -1 && !outx)
+                g0 = 8 * n + (i < 0 ? 0 : 4 * m) + j;  // down table, up table
+        }
+    }
+    jj = jj < 0 ? 0 : (jj >= m ? m - 1 : jj);
+    ii = ii < 0 ? 0 : (ii >= n ? n - 1 : ii);
+    if (outx && outy) {  // corner ghosts are never used; keep plain values
+        su = R(1);
+        sv = R(1);
+        g0 = -1;
+    }
+    if (g0 >= 0) {
+        const int stride = (g0 < 8 * n) ? n : m;
+        w[0] = a.ghost0[g0];
+        w[1] = a.ghost0[g0 + stride];
+        w[2] = a.ghost0[g0 + 2 * stride];
+        w[3] = a.ghost0[g0 + 3 * stride];
+        return;
+    }
+    const size_t o = (size_t)jj * a.ld + ii;
+    w[0] = a.src_w[o];
+    w[1] = su * a.src_w[a.plane + o];
+    w[2] = sv * a.src_w[2 * a.plane + o];
+    w[3] = a.src_w[3 * a.plane + o];
+}
+
+// Index of a cell for reading its previous slopes (wrapped for periodic
+// boundaries, clamped otherwise: non-periodic ghosts' slopes are overridden).
+template <typename R>
+__device__ __forceinline__ size_t slope_index(const StepArgs<R>& a, int j, int i)
+{
+    int jj = j, ii = i;
+    if (jj < 0 || jj >= a.m)
+        jj = (a.bx == -7) ? (jj < 0 ? jj + a.m : jj - a.m) : (jj < 0 ? 0 : a.m - 1);
+    if (ii < 0 || ii >= a.n)
+        ii = (a.by == -7) ? (ii < 0 ? ii + a.n : ii - a.n) : (ii < 0 ? 0 : a.n - 1);
+    jj = jj < 0 ? 0 : (jj >= a.m ? a.m - 1 : jj);
+    ii = ii < 0 ? 0 : (ii >= a.n ? a.n - 1 : ii);
+    return (size_t)jj * a.ld + ii;
+}
+
+template <typename R>
+__device__ __forceinline__ R div_h(R d, R h, R inv_h, int pow2)
+{
+    return pow2 ? d * inv_h : d / h;
+}
+
+// one slope: centred differences sL, sR over h, limited
+template <typename R>
+__device__ __forceinline__ R limit(R wl, R wc, R wr, R h, R inv_h, int pow2, R alpha, int find, R sprev)
+{
+    R sL = div_h(wc - wl, h, inv_h, pow2);
+    R sR = div_h(wr - wc, h, inv_h, pow2);
+    return find ? minmod3(alpha * sL, alpha * sR, sprev) : minmod2(sL, sR);
+}
+
+// Error key of a face: (serial + 1) << 2 | code, max-reduced.
+__device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigned long long serial, int code)
+{
+    if (code)
+        atomicMax(&ctl->key[slot][dir], ((serial + 1ull) << 2) | (unsigned long long)code);
+}
+
+// Solve one face given its two sides in the face's normal frame.
+template <typename R, bool YDIR>
+__device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, const StepArgs<R>& a, FaceOut<R>& o,
+                                          int& iters)
+{
+    int code = ifvar_bad(L, Rr, a.G.eps) ? 1 : 0;
+    Star<R> S;
+    StarInfo st;
+    q1d_star(L, Rr, a.G, S, st);
+    q1d_waves(L, Rr, a.G, S);
+    R D[4], U[4];
+    q1d_derivs(L, Rr, a.G, S, D, U);
+    if (star_dire_check2(U, D, a.G.eps))
+        code = 2;
+    face_flux<R, YDIR>(D, U, a.tau, a.htau, a.G, o);
+    iters = st.iters;
+    return code;
+}
+
+// ---------------------------------------------------------------------------
+// unsplit step: grp_solver_2D_EUL_source.c:146-286
+// ---------------------------------------------------------------------------
+template <typename R, int TJ, int TI>
+struct UnsplitSmem {
+    static constexpr int WJ = TJ + 4, WI = TI + 4;  // values with a 2-cell halo
+    static constexpr int SJ = TJ + 2, SI = TI + 2;  // slopes with a 1-cell halo
+    static constexpr int nW = 4 * WJ * WI;
+    static constexpr int nS = 8 * SJ * SI;
+    static constexpr int nFX = 8 * (TJ + 1) * TI;
+    static constexpr int nFY = 8 * TJ * (TI + 1);
+    static constexpr size_t bytes = sizeof(R) * (size_t)(nW + nS + nFX + nFY);
+};
+
+template <typename R, int TJ, int TI, int NT>
+__global__ void __launch_bounds__(NT) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
+{
+    using SM = UnsplitSmem<R, TJ, TI>;
+    if (halt_prologue(a.ctl, a.seq))
+        return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* W = reinterpret_cast<R*>(smem_raw);
+    R* S = W + SM::nW;
+    R* FX = S + SM::nS;
+    R* FY = FX + SM::nFX;
+    const int tid = threadIdx.x;
+    const int I0 = blockIdx.x * TI, J0 = blockIdx.y * TJ;
+    const int m = a.m, n = a.n, slot = a.seq % 3;
+    constexpr int WJ = SM::WJ, WI = SM::WI, SJ = SM::SJ, SI = SM::SI;
+#define Wx(k, lj, li) W[((k) * WJ + (lj)) * WI + (li)]
+#define Sx(k, sj, si) S[((k) * SJ + (sj)) * SI + (si)]
+#define FXx(k, fj, fi) FX[((k) * (TJ + 1) + (fj)) * TI + (fi)]
+#define FYx(k, gj, gi) FY[((k) * TJ + (gj)) * (TI + 1) + (gi)]
+
+    // 1. values with a 2-cell halo
+    for (int idx = tid; idx < WJ * WI; idx += NT) {
+        int lj = idx / WI, li = idx - lj * WI;
+        R w[4];
+        load_prims(a, J0 - 2 + lj, I0 - 2 + li, w);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            Wx(k, lj, li) = w[k];
+    }
+    __syncthreads();
+
+    // 2. limited slopes of the tile and a 1-cell halo (corners are never used)
+    for (int idx = tid; idx < SJ * SI; idx += NT) {
+        int sj = idx / SI, si = idx - sj * SI;
+        if ((sj == 0 || sj == SJ - 1) && (si == 0 || si == SI - 1))
+            continue;
+        int j = J0 - 1 + sj, i = I0 - 1 + si;
+        size_t o = slope_index(a, j, i);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            R sx = limit(Wx(k, sj, si + 1), Wx(k, sj + 1, si + 1), Wx(k, sj + 2, si + 1), a.hx, a.inv_hx, a.pow2_x,
+                         a.alpha, a.find_x, a.find_x ? a.src_s[k * a.plane + o] : R(0));
+            R sy = limit(Wx(k, sj + 1, si), Wx(k, sj + 1, si + 1), Wx(k, sj + 1, si + 2), a.hy, a.inv_hy, a.pow2_y,
+                         a.alpha, a.find_y, a.find_y ? a.src_t[k * a.plane + o] : R(0));
+            Sx(k, sj, si) = sx;
+            Sx(4 + k, sj, si) = sy;
+        }
+    }
+    __syncthreads();
+
+    // 2b. ghost slopes at non-periodic domain edges
+    if (a.bx != -7) {
+        const int sjg[2] = {(J0 == 0) ? 0 : -1, (m - J0 + 1 <= SJ - 1) ? m - J0 + 1 : -1};
+        for (int idx = tid; idx < 2 * TI; idx += NT) {
+            int side = idx / TI, si = 1 + idx % TI;
+            int sj = sjg[side];
+            if (sj < 0)
+                continue;
+            int se = side == 0 ? sj + 1 : sj - 1;  // edge cell
+            // normal slopes: reflective keeps the edge's u-slope only (left side for -24)
+            bool keep_su = (a.bx == -2) || (a.bx == -24 && side == 0);
+            Sx(0, sj, si) = R(0);
+            Sx(1, sj, si) = keep_su ? Sx(1, se, si) : R(0);
+            Sx(2, sj, si) = R(0);
+            Sx(3, sj, si) = R(0);
+            // transversal slopes: edge cell's, zero for the fixed initial boundary
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                Sx(4 + k, sj, si) = (a.bx == -1) ? R(0) : Sx(4 + k, se, si);
+        }
+    }
+    if (a.by != -7) {
+        const int sig[2] = {(I0 == 0) ? 0 : -1, (n - I0 + 1 <= SI - 1) ? n - I0 + 1 : -1};
+        for (int idx = tid; idx < 2 * TJ; idx += NT) {
+            int side = idx / TJ, sj = 1 + idx % TJ;
+            int si = sig[side];
+            if (si < 0)
+                continue;
+            int se = side == 0 ? si + 1 : si - 1;
+            bool keep_tv = (a.by == -2) || (a.by == -24 && side == 0);
+            Sx(4, sj, si) = R(0);
+            Sx(5, sj, si) = R(0);
+            Sx(6, sj, si) = keep_tv ? Sx(6, sj, se) : R(0);
+            Sx(7, sj, si) = R(0);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                Sx(k, sj, si) = (a.by == -1) ? R(0) : Sx(k, sj, se);
+        }
+    }
+    __syncthreads();
+
+    // 3. faces
+    constexpr int NFX = (TJ + 1) * TI, NFY = TJ * (TI + 1);
+    int my_iters = 0, my_newton = 0;
+    for (int f = tid; f < NFX + NFY; f += NT) {
+        if (f < NFX) {
+            int fj = f / TI, fi = f - fj * TI;
+            int j = J0 + fj, i = I0 + fi;
+            if (j > m || i >= n)
+                continue;
+            Side<R> L, Rr;
+            // left cell (j-1): slopes at (fj, fi+1), values at (fj+1, fi+2)
+            L.drho = Sx(0, fj, fi + 1); L.du = Sx(1, fj, fi + 1); L.dv = Sx(2, fj, fi + 1); L.dp = Sx(3, fj, fi + 1);
+            L.trho = Sx(4, fj, fi + 1); L.tu = Sx(5, fj, fi + 1); L.tv = Sx(6, fj, fi + 1); L.tp = Sx(7, fj, fi + 1);
+            L.rho = Wx(0, fj + 1, fi + 2) + a.hhx * L.drho;
+            L.u = Wx(1, fj + 1, fi + 2) + a.hhx * L.du;
+            L.v = Wx(2, fj + 1, fi + 2) + a.hhx * L.dv;
+            L.p = Wx(3, fj + 1, fi + 2) + a.hhx * L.dp;
+            Rr.drho = Sx(0, fj + 1, fi + 1); Rr.du = Sx(1, fj + 1, fi + 1); Rr.dv = Sx(2, fj + 1, fi + 1); Rr.dp = Sx(3, fj + 1, fi + 1);
+            Rr.trho = Sx(4, fj + 1, fi + 1); Rr.tu = Sx(5, fj + 1, fi + 1); Rr.tv = Sx(6, fj + 1, fi + 1); Rr.tp = Sx(7, fj + 1, fi + 1);
+            Rr.rho = Wx(0, fj + 2, fi + 2) - a.hhx * Rr.drho;
+            Rr.u = Wx(1, fj + 2, fi + 2) - a.hhx * Rr.du;
+            Rr.v = Wx(2, fj + 2, fi + 2) - a.hhx * Rr.dv;
+            Rr.p = Wx(3, fj + 2, fi + 2) - a.hhx * Rr.dp;
+            FaceOut<R> o;
+            int it;
+            int code = solve_face<R, false>(L, Rr, a, o, it);
+            if (it >= 0) {
+                my_newton++;
+                my_iters += it;
+            }
+            report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                FXx(k, fj, fi) = o.F[k];
+                FXx(4 + k, fj, fi) = o.I[k];
+            }
+        } else {
+            int g = f - NFX;
+            int gj = g / (TI + 1), gi = g - gj * (TI + 1);
+            int j = J0 + gj, i = I0 + gi;
+            if (j >= m || i > n)
+                continue;
+            // lower cell (i-1): slopes at (gj+1, gi), values at (gj+2, gi+1); rotated to the +y normal frame:
+            // normal velocity v, tangential -u; normal derivatives are the y-slopes, tangential the negated x-slopes
+            Side<R> D, U;
+            {
+                R t0 = Sx(4, gj + 1, gi), t1 = Sx(5, gj + 1, gi), t2 = Sx(6, gj + 1, gi), t3 = Sx(7, gj + 1, gi);
+                R s0 = Sx(0, gj + 1, gi), s1 = Sx(1, gj + 1, gi), s2 = Sx(2, gj + 1, gi), s3 = Sx(3, gj + 1, gi);
+                R rr = Wx(0, gj + 2, gi + 1) + a.hhy * t0;
+                R uu = Wx(1, gj + 2, gi + 1) + a.hhy * t1;
+                R vv = Wx(2, gj + 2, gi + 1) + a.hhy * t2;
+                R pp = Wx(3, gj + 2, gi + 1) + a.hhy * t3;
+                D.rho = rr; D.u = vv; D.v = -uu; D.p = pp;
+                D.drho = t0; D.du = t2; D.dv = -t1; D.dp = t3;
+                D.trho = -s0; D.tu = -s2; D.tv = s1; D.tp = -s3;
+            }
+            {
+                R t0 = Sx(4, gj + 1, gi + 1), t1 = Sx(5, gj + 1, gi + 1), t2 = Sx(6, gj + 1, gi + 1), t3 = Sx(7, gj + 1, gi + 1);
+                R s0 = Sx(0, gj + 1, gi + 1), s1 = Sx(1, gj + 1, gi + 1), s2 = Sx(2, gj + 1, gi + 1), s3 = Sx(3, gj + 1, gi + 1);
+                R rr = Wx(0, gj + 2, gi + 2) - a.hhy * t0;
+                R uu = Wx(1, gj + 2, gi + 2) - a.hhy * t1;
+                R vv = Wx(2, gj + 2, gi + 2) - a.hhy * t2;
+                R pp = Wx(3, gj + 2, gi + 2) - a.hhy * t3;
+                U.rho = rr; U.u = vv; U.v = -uu; U.p = pp;
+                U.drho = t0; U.du = t2; U.dv = -t1; U.dp = t3;
+                U.trho = -s0; U.tu = -s2; U.tv = s1; U.tp = -s3;
+            }
+            FaceOut<R> o;
+            int it;
+            int code = solve_face<R, true>(D, U, a, o, it);
+            if (it >= 0) {
+                my_newton++;
+                my_iters += it;
+            }
+            report_face(a.ctl, slot, 1, (unsigned long long)j * (n + 1) + i, code);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                FYx(k, gj, gi) = o.F[k];
+                FYx(4 + k, gj, gi) = o.I[k];
+            }
+        }
+    }
+    if (a.stats) {
+        // warp-aggregated statistics
+        __syncwarp();
+        for (int off = 16; off; off >>= 1) {
+            my_newton += __shfl_xor_sync(0xffffffffu, my_newton, off);
+            my_iters += __shfl_xor_sync(0xffffffffu, my_iters, off);
+        }
+        if ((tid & 31) == 0 && my_newton) {
+            atomicAdd(&a.ctl->newton_faces, (unsigned long long)my_newton);
+            atomicAdd(&a.ctl->newton_iters, (unsigned long long)my_iters);
+        }
+    }
+    __syncthreads();
+
+    // 4. conservative update and new slopes
+    unsigned bad = 0;
+    for (int idx = tid; idx < TJ * TI; idx += NT) {
+        int cj = idx / TI, ci = idx - cj * TI;
+        int j = J0 + cj, i = I0 + ci;
+        if (j >= m || i >= n)
+            continue;
+        const size_t o = (size_t)j * a.ld + i;
+        R rho = Wx(0, cj + 2, ci + 2), uu = Wx(1, cj + 2, ci + 2), vv = Wx(2, cj + 2, ci + 2);
+        R E = a.src_w[4 * a.plane + o];
+        R mom_x = rho * uu - a.nu * (FXx(1, cj + 1, ci) - FXx(1, cj, ci)) - a.mu * (FYx(1, cj, ci + 1) - FYx(1, cj, ci));
+        R mom_y = rho * vv - a.nu * (FXx(2, cj + 1, ci) - FXx(2, cj, ci)) - a.mu * (FYx(2, cj, ci + 1) - FYx(2, cj, ci));
+        R ene = rho * E - a.nu * (FXx(3, cj + 1, ci) - FXx(3, cj, ci)) - a.mu * (FYx(3, cj, ci + 1) - FYx(3, cj, ci));
+        rho += -a.nu * (FXx(0, cj + 1, ci) - FXx(0, cj, ci)) - a.mu * (FYx(0, cj, ci + 1) - FYx(0, cj, ci));
+        R un = mom_x / rho, vn = mom_y / rho, En = ene / rho;
+        R pn = (ene - R(0.5) * mom_x * un - R(0.5) * mom_y * vn) * a.G.gm1;
+        if (pn < a.G.eps || rho < a.G.eps)
+            bad = 1;
+        a.dst_w[o] = rho;
+        a.dst_w[a.plane + o] = un;
+        a.dst_w[2 * a.plane + o] = vn;
+        a.dst_w[3 * a.plane + o] = pn;
+        a.dst_w[4 * a.plane + o] = En;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            a.dst_s[k * a.plane + o] = div_h(FXx(4 + k, cj + 1, ci) - FXx(4 + k, cj, ci), a.hx, a.inv_hx, a.pow2_x);
+            a.dst_t[k * a.plane + o] = div_h(FYx(4 + k, cj, ci + 1) - FYx(4 + k, cj, ci), a.hy, a.inv_hy, a.pow2_y);
+        }
+    }
+    if (bad)
+        atomicOr(&a.ctl->upd_bad[slot], 1u);
+#undef Wx
+#undef Sx
+#undef FXx
+#undef FYx
+}
+
+// ---------------------------------------------------------------------------
+// split sweeps: grp_solver_2D_split_EUL_source.c:214-303.  YDIR = 0: x-sweep
+// (x-faces, half time step, s updated); YDIR = 1: y-sweep (y-faces, t updated).
+// No transversal derivatives (Transversal = false).  Written in the sweep's
+// own coordinates: "a" is the sweep axis, "b" the other one.
+// ---------------------------------------------------------------------------
+template <typename R, int TJ, int TI>
+struct SweepSmem {
+    // TA cells along the sweep axis with a 2-cell halo, TB cells across
+    static constexpr size_t bytes(int TA, int TB)
+    {
+        return sizeof(R) * (size_t)(4 * (TA + 4) * TB + 4 * (TA + 2) * TB + 8 * (TA + 1) * TB);
+    }
+};
+
+template <typename R, int YDIR, int TJ, int TI, int NT>
+__global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R> a)
+{
+    if (halt_prologue(a.ctl, a.seq))
+        return;
+    // sweep axis length TA (with halo) and cross length TB
+    constexpr int TA = YDIR ? TI : TJ;
+    constexpr int TB = YDIR ? TJ : TI;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* W = reinterpret_cast<R*>(smem_raw);   // [4][TA+4][TB]
+    R* S = W + 4 * (TA + 4) * TB;            // [4][TA+2][TB]
+    R* F = S + 4 * (TA + 2) * TB;            // [8][TA+1][TB]
+    const int tid = threadIdx.x;
+    const int I0 = blockIdx.x * TI, J0 = blockIdx.y * TJ;
+    const int m = a.m, n = a.n, slot = a.seq % 3;
+    const int A0 = YDIR ? I0 : J0, B0 = YDIR ? J0 : I0;
+    const int NA = YDIR ? n : m, NB = YDIR ? m : n;
+    const int bnd = YDIR ? a.by : a.bx;
+    const R h = YDIR ? a.hy : a.hx, inv_h = YDIR ? a.inv_hy : a.inv_hx;
+    const int pow2 = YDIR ? a.pow2_y : a.pow2_x;
+    const R hh = YDIR ? a.hhy : a.hhx;
+    const R fac = YDIR ? a.mu : a.nu;
+    const int find = YDIR ? a.find_y : a.find_x;
+    const R* src_sl = YDIR ? a.src_t : a.src_s;
+    R* dst_sl = YDIR ? a.dst_t : a.dst_s;
+#define Wv(k, la, lb) W[((k) * (TA + 4) + (la)) * TB + (lb)]
+#define Sv(k, sa, lb) S[((k) * (TA + 2) + (sa)) * TB + (lb)]
+#define Fv(k, fa, lb) F[((k) * (TA + 1) + (fa)) * TB + (lb)]
+
+    for (int idx = tid; idx < (TA + 4) * TB; idx += NT) {
+        int la, lb;
+        if (YDIR) { lb = idx / (TA + 4); la = idx - lb * (TA + 4); }
+        else { la = idx / TB; lb = idx - la * TB; }
+        int ca = A0 - 2 + la, cb = B0 + lb;
+        int j = YDIR ? cb : ca, i = YDIR ? ca : cb;
+        R w[4];
+        load_prims(a, j, i, w);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            Wv(k, la, lb) = w[k];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < (TA + 2) * TB; idx += NT) {
+        int sa, lb;
+        if (YDIR) { lb = idx / (TA + 2); sa = idx - lb * (TA + 2); }
+        else { sa = idx / TB; lb = idx - sa * TB; }
+        int ca = A0 - 1 + sa, cb = B0 + lb;
+        int j = YDIR ? cb : ca, i = YDIR ? ca : cb;
+        if (cb >= NB)
+            continue;
+        size_t o = slope_index(a, j, i);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            Sv(k, sa, lb) = limit(Wv(k, sa, lb), Wv(k, sa + 1, lb), Wv(k, sa + 2, lb), h, inv_h, pow2, a.alpha, find,
+                                  find ? src_sl[k * a.plane + o] : R(0));
+    }
+    __syncthreads();
+    if (bnd != -7) {
+        const int sg[2] = {(A0 == 0) ? 0 : -1, (NA - A0 + 1 <= TA + 1) ? NA - A0 + 1 : -1};
+        const int keep = YDIR ? 2 : 1;  // reflective keeps the normal velocity's slope
+        for (int idx = tid; idx < 2 * TB; idx += NT) {
+            int side = idx / TB, lb = idx % TB;
+            int sa = sg[side];
+            if (sa < 0)
+                continue;
+            int se = side == 0 ? sa + 1 : sa - 1;
+            bool kp = (bnd == -2) || (bnd == -24 && side == 0);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                Sv(k, sa, lb) = (kp && k == keep) ? Sv(k, se, lb) : R(0);
+        }
+    }
+    __syncthreads();
+
+    int my_iters = 0, my_newton = 0;
+    for (int f = tid; f < (TA + 1) * TB; f += NT) {
+        int fa, lb;
+        if (YDIR) { lb = f / (TA + 1); fa = f - lb * (TA + 1); }
+        else { fa = f / TB; lb = f - fa * TB; }
+        int ca = A0 + fa, cb = B0 + lb;
+        if (ca > NA || cb >= NB)
+            continue;
+        R s0 = Sv(0, fa, lb), s1 = Sv(1, fa, lb), s2 = Sv(2, fa, lb), s3 = Sv(3, fa, lb);
+        R r0 = Sv(0, fa + 1, lb), r1 = Sv(1, fa + 1, lb), r2 = Sv(2, fa + 1, lb), r3 = Sv(3, fa + 1, lb);
+        R lr = Wv(0, fa + 1, lb) + hh * s0, lu = Wv(1, fa + 1, lb) + hh * s1;
+        R lv = Wv(2, fa + 1, lb) + hh * s2, lp = Wv(3, fa + 1, lb) + hh * s3;
+        R rr = Wv(0, fa + 2, lb) - hh * r0, ru = Wv(1, fa + 2, lb) - hh * r1;
+        R rv = Wv(2, fa + 2, lb) - hh * r2, rp = Wv(3, fa + 2, lb) - hh * r3;
+        Side<R> L, Rr;
+        if (!YDIR) {
+            L.rho = lr; L.u = lu; L.v = lv; L.p = lp; L.drho = s0; L.du = s1; L.dv = s2; L.dp = s3;
+            Rr.rho = rr; Rr.u = ru; Rr.v = rv; Rr.p = rp; Rr.drho = r0; Rr.du = r1; Rr.dv = r2; Rr.dp = r3;
+        } else {
+            L.rho = lr; L.u = lv; L.v = -lu; L.p = lp; L.drho = s0; L.du = s2; L.dv = -s1; L.dp = s3;
+            Rr.rho = rr; Rr.u = rv; Rr.v = -ru; Rr.p = rp; Rr.drho = r0; Rr.du = r2; Rr.dv = -r1; Rr.dp = r3;
+        }
+        L.trho = L.tu = L.tv = L.tp = R(0);
+        Rr.trho = Rr.tu = Rr.tv = Rr.tp = R(0);
+        FaceOut<R> o;
+        int it, code;
+        if (YDIR)
+            code = solve_face<R, true>(L, Rr, a, o, it);
+        else
+            code = solve_face<R, false>(L, Rr, a, o, it);
+        if (it >= 0) {
+            my_newton++;
+            my_iters += it;
+        }
+        int j = YDIR ? cb : ca, i = YDIR ? ca : cb;
+        unsigned long long serial = YDIR ? (unsigned long long)j * (n + 1) + i : (unsigned long long)i * (m + 1) + j;
+        report_face(a.ctl, slot, YDIR, serial, code);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            Fv(k, fa, lb) = o.F[k];
+            Fv(4 + k, fa, lb) = o.I[k];
+        }
+    }
+    if (a.stats) {
+        __syncwarp();
+        for (int off = 16; off; off >>= 1) {
+            my_newton += __shfl_xor_sync(0xffffffffu, my_newton, off);
+            my_iters += __shfl_xor_sync(0xffffffffu, my_iters, off);
+        }
+        if ((tid & 31) == 0 && my_newton) {
+            atomicAdd(&a.ctl->newton_faces, (unsigned long long)my_newton);
+            atomicAdd(&a.ctl->newton_iters, (unsigned long long)my_iters);
+        }
+    }
+    __syncthreads();
+
+    unsigned bad = 0;
+    for (int idx = tid; idx < TA * TB; idx += NT) {
+        int ca_l, lb;
+        if (YDIR) { lb = idx / TA; ca_l = idx - lb * TA; }
+        else { ca_l = idx / TB; lb = idx - ca_l * TB; }
+        int ca = A0 + ca_l, cb = B0 + lb;
+        if (ca >= NA || cb >= NB)
+            continue;
+        int j = YDIR ? cb : ca, i = YDIR ? ca : cb;
+        const size_t o = (size_t)j * a.ld + i;
+        R rho = Wv(0, ca_l + 2, lb);
+        R uu = Wv(1, ca_l + 2, lb), vv = Wv(2, ca_l + 2, lb);
+        R E = a.src_w[4 * a.plane + o];
+        R mom_x = rho * uu - fac * (Fv(1, ca_l + 1, lb) - Fv(1, ca_l, lb));
+        R mom_y = rho * vv - fac * (Fv(2, ca_l + 1, lb) - Fv(2, ca_l, lb));
+        R ene = rho * E - fac * (Fv(3, ca_l + 1, lb) - Fv(3, ca_l, lb));
+        rho += -fac * (Fv(0, ca_l + 1, lb) - Fv(0, ca_l, lb));
+        R un = mom_x / rho, vn = mom_y / rho, En = ene / rho;
+        R pn = (ene - R(0.5) * mom_x * un - R(0.5) * mom_y * vn) * a.G.gm1;
+        if (pn < a.G.eps || rho < a.G.eps)
+            bad = 1;
+        a.dst_w[o] = rho;
+        a.dst_w[a.plane + o] = un;
+        a.dst_w[2 * a.plane + o] = vn;
+        a.dst_w[3 * a.plane + o] = pn;
+        a.dst_w[4 * a.plane + o] = En;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            dst_sl[k * a.plane + o] = div_h(Fv(4 + k, ca_l + 1, lb) - Fv(4 + k, ca_l, lb), h, inv_h, pow2);
+    }
+    if (bad)
+        atomicOr(&a.ctl->upd_bad[slot], 1u);
+#undef Wv
+#undef Sv
+#undef Fv
+}
+
+}  // namespace hydro

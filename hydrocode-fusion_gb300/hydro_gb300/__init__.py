@@ -1,0 +1,171 @@
+"""Python access to libhydro_gb300.so (ctypes over the C ABI in include/hydro_gb300.h).
+
+The library is the product: GB300 (sm_103a) kernels behind the reference's
+scheme entry points.  This module only loads it and moves numpy arrays across
+the C ABI; there is no Python or CPU fallback -- a missing or unloadable
+library raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libhydro_gb300.so")
+NCONF = 400
+
+FORM_FP64 = 0
+FORM_FP32 = 1
+FORM_FP32_LEARNED = 2
+
+_dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+
+class RunInfo(ctypes.Structure):
+    _fields_ = [
+        ("k_out", ctypes.c_int),
+        ("steps_done", ctypes.c_int),
+        ("sweeps_launched", ctypes.c_int),
+        ("halted", ctypes.c_int),
+        ("error_code_x", ctypes.c_int),
+        ("error_code_y", ctypes.c_int),
+        ("time", ctypes.c_double),
+        ("tau", ctypes.c_double),
+        ("gpu_ms", ctypes.c_double),
+        ("newton_faces", ctypes.c_ulonglong),
+        ("newton_iters", ctypes.c_ulonglong),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def build(jobs: int = 4) -> str:
+    """Compile the library in-tree (nvcc, sm_103a) and return its path."""
+    subprocess.run(["make", "-s", "-j", str(jobs), "-C", PKG_DIR], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load the library once; raise if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libhydro_gb300.so not built: {LIB_PATH} (run make -C {PKG_DIR})")
+    L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
+    L.hydro2d_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.hydro2d_create.restype = ctypes.c_int
+    L.hydro2d_destroy.argtypes = [ctypes.c_void_p]
+    L.hydro2d_destroy.restype = None
+    L.hydro2d_upload.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.c_void_p, ctypes.c_double]
+    L.hydro2d_upload.restype = ctypes.c_int
+    L.hydro2d_download.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp]
+    L.hydro2d_download.restype = ctypes.c_int
+    L.hydro2d_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RunInfo)]
+    L.hydro2d_run.restype = ctypes.c_int
+    L.hydro_gb300_last_error.restype = ctypes.c_char_p
+    L.hydro_gb300_kernel_launches.restype = ctypes.c_ulonglong
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().hydro_gb300_last_error().decode()
+
+
+def kernel_launches() -> int:
+    return int(lib().hydro_gb300_kernel_launches())
+
+
+def config_2d(**kw) -> np.ndarray:
+    """config[] for a 2D Eulerian run as the reference's config_check leaves it
+    (src/file_io/config_handle.c:39-152); keyword overrides by name."""
+    c = np.full(NCONF, np.inf)
+    c[0] = 2
+    c[2] = 1; c[8] = 0; c[30] = 0; c[31] = 0; c[32] = 1; c[33] = 0; c[40] = 0
+    c[41] = 1.9; c[42] = 1; c[53] = 0; c[60] = 0; c[61] = 0; c[70] = 0
+    c[110] = 0.72; c[210] = 0.0; c[211] = 0.0; c[212] = 0.0
+    c[4] = 1e-9; c[6] = 1.4; c[7] = 0.45
+    names = {"t_all": 1, "eps": 4, "steps": 5, "gamma": 6, "cfl": 7, "hx": 10, "hy": 11,
+             "tau": 16, "bx": 17, "by": 18, "split": 33, "alpha": 41, "form": 300}
+    for k, v in kw.items():
+        c[names[k]] = v
+    if not (math.isfinite(c[1]) and c[1] >= 0.0):
+        c[1] = np.inf
+    c[20] = c[10]
+    return c
+
+
+def config_1d(**kw) -> np.ndarray:
+    c = config_2d(**kw)
+    c[0] = 1
+    if "cfl" not in kw:
+        c[7] = 0.9
+    return c
+
+
+class Solver2D:
+    """Device-resident 2D solver (hydro2d_* in the C ABI).
+
+    Arrays are x-major numpy arrays of shape (m, n): value of cell (x=j, y=i) at [j, i].
+    """
+
+    def __init__(self, m: int, n: int, form: int = FORM_FP64):
+        self.m, self.n, self.form = m, n, form
+        h = ctypes.c_void_p()
+        if lib().hydro2d_create(ctypes.byref(h), m, n, form) != 0:
+            raise RuntimeError("hydro2d_create failed: " + last_error())
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().hydro2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, rho, u, v, p, E=None, gamma=1.4):
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (rho, u, v, p)]
+        for a in arrs:
+            assert a.shape == (self.m, self.n)
+        e = None if E is None else np.ascontiguousarray(E, np.float64)
+        rc = lib().hydro2d_upload(self._h, *arrs, None if e is None else e.ctypes.data, gamma)
+        if rc != 0:
+            raise RuntimeError("upload failed: " + last_error())
+
+    def download(self):
+        out = [np.empty((self.m, self.n)) for _ in range(5)]
+        if lib().hydro2d_download(self._h, *out) != 0:
+            raise RuntimeError("download failed: " + last_error())
+        return dict(zip(("rho", "u", "v", "p", "E"), out))
+
+    def run(self, cfg, split=False, stats=False) -> RunInfo:
+        cfg = np.ascontiguousarray(cfg, np.float64)
+        info = RunInfo()
+        if lib().hydro2d_run(self._h, cfg, len(cfg), int(bool(split)), int(bool(stats)), ctypes.byref(info)) != 0:
+            raise RuntimeError("run failed: " + last_error())
+        return info
+
+
+def run_2d(rho, u, v, p, cfg, split=False, form=FORM_FP64, stats=False):
+    """Upload, run, download; returns (state dict, RunInfo)."""
+    m, n = np.shape(rho)
+    s = Solver2D(m, n, form)
+    try:
+        s.upload(rho, u, v, p, None, float(cfg[6]))
+        info = s.run(cfg, split=split, stats=stats)
+        return s.download(), info
+    finally:
+        s.close()

@@ -1,0 +1,120 @@
+/*
+ * hydro_gb300.h -- C ABI of libhydro_gb300.so, the GB300 (sm_103a) drop-in for
+ * HydroCODE's Eulerian Godunov/GRP scheme call (1D and 2D structured,
+ * single-fluid, ideal gas).
+ *
+ * Part 1 is the drop-in boundary: the four scheme entry points with the
+ * signatures, argument meaning, ownership and side effects of the reference's
+ * src/include/finite_volume.h.  Inputs come from the global `double config[]`
+ * (defined by the caller, as the reference's drivers do; the library carries a
+ * weak fallback definition), the caller owns every array, and results are
+ * written back exactly where the reference writes them.
+ *
+ * Part 2 is a native API with no reference counterpart: a device-resident 2D
+ * solver handle (used by the tests and the benchmark), the precision/guess
+ * form selector and error reporting.
+ *
+ * All calls are synchronous, run on the current CUDA device and, like the
+ * reference, are not re-entrant (one global config[]).
+ */
+#ifndef HYDRO_GB300_H
+#define HYDRO_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef N_CONF
+#define N_CONF 400
+#endif
+
+/* The caller's configuration array (reference: src/include/var_struc.h:44,
+ * defined in src/hydrocode_2D/hydrocode.c:123 and src/hydrocode_1D/hydrocode.c:111).
+ * Indices follow the reference's doc/config.csv; this library additionally reads
+ *   config[300]  precision/guess form of the 2D scheme (HYDRO_FORM_*; INFINITY or
+ *                absent = HYDRO_FORM_FP64, the reference's arithmetic). */
+extern double config[];
+
+/* Same member order as the reference's struct cell_var_stru
+ * (src/include/var_struc.h:61-74, single-fluid build). */
+struct cell_var_stru {
+    double **E;
+    double **RHO, **U, **V, **P;
+    double *d_rho, *d_u, *d_v, *d_p;
+    double **s_rho, **s_u, **s_v, **s_p;
+    double **t_rho, **t_u, **t_v, **t_p;
+    double **rhoIx, **uIx, **vIx, **pIx;
+    double **rhoIy, **uIy, **vIy, **pIy;
+    double **F_rho, **F_e, **F_u, **F_v;
+    double **G_rho, **G_e, **G_u, **G_v;
+};
+
+/* ---- Part 1: drop-in scheme entry points --------------------------------- */
+
+/* 1D first-order Godunov scheme with the exact Riemann solver.
+ * Replaces src/finite_volume/godunov_solver_EUL_source.c:27 (declared at
+ * src/include/finite_volume.h:33).  CV.RHO/U/P/E[k][j], k < *N_plot. */
+void Godunov_solver_EUL_source(const int m, struct cell_var_stru CV, double *cpu_time, int *N_plot,
+                               double time_plot[]);
+
+/* 1D second-order direct Eulerian GRP scheme.
+ * Replaces src/finite_volume/grp_solver_EUL_source.c:27 (finite_volume.h:37). */
+void GRP_solver_EUL_source(const int m, struct cell_var_stru CV, double *cpu_time, int *N_plot,
+                           double time_plot[]);
+
+/* 2D unsplit GRP scheme.  CV[k].RHO/U/V/P/E[j][i] (x-major), k < N_T.
+ * Replaces src/finite_volume/grp_solver_2D_EUL_source.c:75 (finite_volume.h:43-44). */
+void GRP_solver_2D_EUL_source(const int m, const int n, struct cell_var_stru *CV, double **X, double **Y,
+                              double *cpu_time, const char *problem, int N_T, int *N_plot, double time_plot[]);
+
+/* 2D dimension-split GRP scheme.
+ * Replaces src/finite_volume/grp_solver_2D_split_EUL_source.c:75 (finite_volume.h:48-49). */
+void GRP_solver_2D_split_EUL_source(const int m, const int n, struct cell_var_stru *CV, double **X, double **Y,
+                                    double *cpu_time, const char *problem, int N_T, int *N_plot,
+                                    double time_plot[]);
+
+/* ---- Part 2: native API (no reference counterpart) ------------------------ */
+
+enum {
+    HYDRO_FORM_FP64 = 0,         /* reference arithmetic in FP64 (parity form) */
+    HYDRO_FORM_FP32 = 1,         /* FP32 state and fluxes, FP64 near-vacuum Newton */
+    HYDRO_FORM_FP32_LEARNED = 2  /* FP32 form with the learned Newton starting pressure */
+};
+
+typedef struct hydro2d hydro2d_t;
+
+/* Outcome of a run, in the reference's terms. */
+typedef struct {
+    int k_out;            /* value the reference writes to config[5] */
+    int steps_done;       /* time steps whose update was kept */
+    int sweeps_launched;  /* kernel launches of the time loop */
+    int halted;           /* 0 ran to the end, 1 aborted (last step discarded), 2 stopped after a step */
+    int error_code_x;     /* last failing x-face code (0 none, 1 reconstruction, 2 GRP check) */
+    int error_code_y;
+    double time;          /* final time (time_plot[nt]) */
+    double tau;           /* last time step */
+    double gpu_ms;        /* device time of the time loop (CUDA events) */
+    unsigned long long newton_faces, newton_iters;  /* exact-solver statistics (when enabled) */
+} hydro_run_info;
+
+/* Create a solver for an m (x) by n (y) grid in the given form. 0 on success. */
+int hydro2d_create(hydro2d_t **out, int m, int n, int form);
+void hydro2d_destroy(hydro2d_t *h);
+/* Upload an x-major (value of cell (j,i) at [j*n+i]) FP64 state; E may be NULL,
+ * then E = 0.5 u^2 + p/(gamma-1)/rho + 0.5 v^2 as the reference's driver computes it. */
+int hydro2d_upload(hydro2d_t *h, const double *rho, const double *u, const double *v, const double *p,
+                   const double *E, double gamma);
+int hydro2d_download(hydro2d_t *h, double *rho, double *u, double *v, double *p, double *E);
+/* Run the time loop configured by cfg[0..ncfg) (config[] semantics) from the
+ * uploaded state: split = 0 unsplit, 1 dimension split.  stats != 0 counts
+ * Newton faces/iterations. */
+int hydro2d_run(hydro2d_t *h, const double *cfg, int ncfg, int split, int stats, hydro_run_info *info);
+/* Number of CUDA kernels launched by this library since load (all solvers). */
+unsigned long long hydro_gb300_kernel_launches(void);
+/* Message of the last failing call in this thread ("" if none). */
+const char *hydro_gb300_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

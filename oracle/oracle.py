@@ -23,6 +23,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libhydro_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libhydro_ref.so")
+# Where oracle/Makefile finds the reference sources (only needed to build REF_SO).
+REF_TREE = os.environ.get("HYDRO_REFERENCE", "/root/reference")
 NCONF = 400
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -30,10 +32,14 @@ _int = ctypes.c_int
 _dbl = ctypes.c_double
 
 
+def reference_available() -> bool:
+    return os.path.isdir(os.path.join(REF_TREE, "src", "finite_volume"))
+
+
 def build(ref: bool = False) -> None:
     """Compile the port (and the reference lib if asked and possible)."""
-    targets = ["port"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+    targets = ["port"] + (["ref"] if ref and reference_available() else [])
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_TREE}"] + targets, check=True)
 
 
 def default_config_2d(**kw) -> np.ndarray:
