@@ -120,35 +120,33 @@ template <typename R>
 __device__ __forceinline__ void load_prims(const StepArgs<R>& a, int j, int i, R w[4])
 {
     const int m = a.m, n = a.n;
+    // periodic directions first: a wrapped halo cell is a real cell whose own
+    // ghosts in the other direction follow that direction's boundary rule
+    if (a.bx == -7 && (j < 0 || j >= m))
+        j = j < 0 ? j + m : j - m;
+    if (a.by == -7 && (i < 0 || i >= n))
+        i = i < 0 ? i + n : i - n;
     bool outx = (j < 0 || j >= m), outy = (i < 0 || i >= n);
     int jj = j, ii = i;
     R su = R(1), sv = R(1);
     int g0 = -1;  // index into the -1 (initial value) ghost table
     if (outx) {
-        if (a.bx == -7) {
-            jj = j < 0 ? j + m : j - m;
-        } else {
-            jj = j < 0 ? 0 : m - 1;
-            if (a.bx == -2 || (a.bx == -24 && j < 0))
-                su = R(-1);
-            if (a.bx == -1 && !outy)
-                g0 = (j < 0 ? 0 : 4 * n) + i;  // left table, right table
-        }
+        jj = j < 0 ? 0 : m - 1;
+        if (a.bx == -2 || (a.bx == -24 && j < 0))
+            su = R(-1);
+        if (a.bx == -1 && !outy)
+            g0 = (j < 0 ? 0 : 4 * n) + i;  // left table, right table
     }
     if (outy) {
-        if (a.by == -7) {
-            ii = i < 0 ? i + n : i - n;
-        } else {
-            ii = i < 0 ? 0 : n - 1;
-            if (a.by == -2 || (a.by == -24 && i < 0))
-                sv = R(-1);
-            if (a.by == -1 && !outx)
-                g0 = 8 * n + (i < 0 ? 0 : 4 * m) + j;  // down table, up table
-        }
+        ii = i < 0 ? 0 : n - 1;
+        if (a.by == -2 || (a.by == -24 && i < 0))
+            sv = R(-1);
+        if (a.by == -1 && !outx)
+            g0 = 8 * n + (i < 0 ? 0 : 4 * m) + j;  // down table, up table
     }
     jj = jj < 0 ? 0 : (jj >= m ? m - 1 : jj);
     ii = ii < 0 ? 0 : (ii >= n ? n - 1 : ii);
-    if (outx && outy) {  // corner ghosts are never used; keep plain values
+    if (outx && outy) {  // corners of two non-periodic boundaries are never used
         su = R(1);
         sv = R(1);
         g0 = -1;

@@ -109,6 +109,11 @@ int hydro2d_download(hydro2d_t *h, double *rho, double *u, double *v, double *p,
  * uploaded state: split = 0 unsplit, 1 dimension split.  stats != 0 counts
  * Newton faces/iterations. */
 int hydro2d_run(hydro2d_t *h, const double *cfg, int ncfg, int split, int stats, hydro_run_info *info);
+/* 1D run (order 1 = Godunov, 2 = GRP) of an m-cell tube held in host arrays
+ * (final state written back; E may be NULL, then the driver's formula is used),
+ * configured by cfg[] like the 1D scheme entry points, with no plot snapshots. */
+int hydro1d_run(int m, double *rho, double *u, double *p, double *E, const double *cfg, int ncfg, int order,
+                hydro_run_info *info);
 /* Number of CUDA kernels launched by this library since load (all solvers). */
 unsigned long long hydro_gb300_kernel_launches(void);
 /* Message of the last failing call in this thread ("" if none). */

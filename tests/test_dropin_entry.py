@@ -1,0 +1,58 @@
+"""The reference's scheme entry points, called the way its drivers call them
+(global config[], caller-owned struct cell_var_stru arrays), against the
+reference's golden output (plot snapshots included)."""
+import os
+
+import numpy as np
+import pytest
+
+from cvstruct import call_1d, call_2d
+from helpers import rel_l1
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = 1e-12
+
+
+@pytest.mark.gpu
+def test_2d_entry_with_plot_snapshots(gpu_lib):
+    hg = gpu_lib
+    d = np.load(os.path.join(GOLD, "runs_2d.npz"))
+    rho, u, v, p = d["snap/in"]
+    cfg = d["snap/cfg"].copy()
+    data, nplot, time_plot, k_out = call_2d(hg.lib(), rho, u, v, p, 1.4, cfg, plot_times=[0.02, 0.05])
+    snaps = d["snap/snaps"]
+    assert nplot == snaps.shape[0]
+    assert k_out == d["snap/meta"][0] and time_plot[nplot - 1] == d["snap/meta"][1]
+    for k in range(nplot):
+        for f in range(5):
+            assert rel_l1(data[k, f], snaps[k, f]) <= TOL, (k, f)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("split", [0, 1])
+def test_2d_entry_matches_oracle(gpu_lib, port, split):
+    hg = gpu_lib
+    from hydro_gb300 import cases
+
+    m, n = 23, 19
+    rho, u, v, p = cases.four_quadrant(m, n, 4)
+    cfg = hg.config_2d(t_all=0.04, steps=1000, hx=1 / m, hy=1 / n, bx=-4, by=-2, split=split)
+    data, nplot, time_plot, k_out = call_2d(hg.lib(), rho, u, v, p, 1.4, cfg, split=split)
+    want = port.run_2d(rho, u, v, p, cfg, split=split)
+    assert k_out == want["steps"] and time_plot[nplot - 1] == want["time"]
+    for f, key in enumerate(("rho", "u", "v", "p", "E")):
+        assert rel_l1(data[nplot - 1, f], want[key]) <= TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2])
+def test_1d_entry_sod(gpu_lib, order):
+    hg = gpu_lib
+    from hydro_gb300 import cases
+
+    d = np.load(os.path.join(GOLD, "runs_1d.npz"))
+    rho, u, p = cases.sod(400)
+    data, nplot, time_plot, k_out = call_1d(hg.lib(), rho, u, p, 1.4, d[f"sod{order}/cfg"].copy(), order)
+    assert nplot == 2 and k_out == d[f"sod{order}/meta"][0] and time_plot[1] == d[f"sod{order}/meta"][1]
+    for f, key in enumerate(("rho", "u", "p", "E")):
+        assert rel_l1(data[f, 1], d[f"sod{order}/{key}"]) <= TOL
