@@ -116,6 +116,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the kernel-variant autotuner")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -152,6 +153,11 @@ def main():
 
     s = hg.Solver2D(m, n, form)
     s.upload(rho, u, v, p)
+    tune = None
+    if not args.no_tune:
+        best, times = s.autotune(cfg_w, steps=3)
+        tune = {"best": best, "ms_per_3_steps": times}
+    variant = s.variant()
     s.run(cfg_w)                      # warm-up steps
     s.upload(rho, u, v, p)
     torch.cuda.synchronize()
@@ -167,6 +173,10 @@ def main():
     # FP64 parity form, same grid
     s64 = hg.Solver2D(m, n, hg.FORM_FP64)
     s64.upload(rho, u, v, p)
+    tune64 = None
+    if not args.no_tune and args.fp64_steps > 0:
+        best64, times64 = s64.autotune(hg.config_2d(t_all=-1, steps=2, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), steps=2)
+        tune64 = {"best": best64, "ms_per_2_steps": times64}
     s64.run(hg.config_2d(t_all=-1, steps=3, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4))
     s64.upload(rho, u, v, p)
     i64 = s64.run(hg.config_2d(t_all=-1, steps=args.fp64_steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), stats=True)
@@ -188,12 +198,14 @@ def main():
     line = {"metric": metric, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload, "form": "fp32", "grid": [m, n], "l2": "inputs larger than L2 (13 planes x 4 B x 16.8M cells)"},
+            "config": {"workload": workload, "form": "fp32", "grid": [m, n], "l2": "inputs larger than L2 (13 planes x 4 B x 16.8M cells)",
+                       "kernel_variant": variant, "autotune": tune},
             "roofline": roof, "cpu_baseline": cpu, "gpu_launches": int(launches),
             "fp64": {"value": fp64_rate, "unit": "cell-updates/s", "steps": args.fp64_steps,
                      "ms_per_step": i64.gpu_ms / args.fp64_steps,
                      "newton_faces_per_step": i64.newton_faces / args.fp64_steps,
-                     "newton_iters_per_face": (i64.newton_iters / i64.newton_faces) if i64.newton_faces else 0.0},
+                     "newton_iters_per_face": (i64.newton_iters / i64.newton_faces) if i64.newton_faces else 0.0,
+                     "autotune": tune64},
             "clocks": cs.summary()}
     if rank == 0:
         print(json.dumps(line))

@@ -285,6 +285,20 @@ int hydro2d_run(hydro2d_t* h, const double* cfg, int ncfg, int split, int stats,
     return h->s->run(rc, split, stats, tp, 2, 2, nullptr, info, &nt);
 }
 
+int hydro2d_num_variants(hydro2d_t* h) { return h->s->num_variants(); }
+int hydro2d_set_variant(hydro2d_t* h, int v) { return h->s->set_variant(v); }
+int hydro2d_get_variant(hydro2d_t* h, int* shape)
+{
+    int v = h->s->get_variant();
+    if (shape)
+        h->s->variant_shape(v, shape);
+    return v;
+}
+int hydro2d_autotune(hydro2d_t* h, const double* cfg, int ncfg, int steps, float* times_ms)
+{
+    return h->s->autotune(run_config_from(cfg, ncfg), steps, times_ms);
+}
+
 void GRP_solver_2D_EUL_source(const int m, const int n, struct cell_var_stru* CV, double** X, double** Y,
                               double* cpu_time, const char* problem, int N_T, int* N_plot, double time_plot[])
 {

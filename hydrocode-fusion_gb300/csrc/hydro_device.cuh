@@ -260,16 +260,12 @@ template <> struct StarPolicy<double> {
     }
 };
 
-__device__ __forceinline__ void gas64_from(const Gas<float>& G, Gas<double>& D)
-{
-    double g = G.g64, zeta = (g - 1.0) / (g + 1.0);
-    D.g = g;
-    D.gm1 = g - 1.0;
-    D.zeta = zeta;
-    D.mu = (g - 1.0) / (2.0 * g);
-    D.nu = (g + 1.0) / (2.0 * g);
-    D.eps = G.eps64;
-}
+
+// FP64 reference iteration used by the FP32 form for hard faces; kept out of
+// line so its FP64 register footprint does not burden the common path.
+static __device__ __noinline__ void exact_riemann_fp64_fallback(float uL, float uR, float pL, float pR, float cL, float cR,
+                                                         double g, double eps, float& u_star, float& p_star,
+                                                         StarInfo& st);
 
 template <> struct StarPolicy<float> {
     static __device__ __forceinline__ bool uniform(float dist, float scale, const Gas<float>& G)
@@ -312,17 +308,9 @@ template <> struct StarPolicy<float> {
         }
         st.iters = it;
         if (!(gap <= tol) || p < 1e-3f * fminf(pL, pR)) {
-            Gas<double> D;
-            gas64_from(G, D);
-            double us, ps;
-            StarInfo s2;
-            exact_riemann<double>((double)uL, (double)uR, (double)pL, (double)pR, (double)cL, (double)cR, D.eps, 500,
-                                  D, us, ps, s2);
-            u_star = (float)us;
-            p_star = (float)ps;
-            st.crw0 = s2.crw0;
-            st.crw1 = s2.crw1;
-            st.iters += s2.iters;
+            int it32 = st.iters;
+            exact_riemann_fp64_fallback(uL, uR, pL, pR, cL, cR, G.g64, G.eps64, u_star, p_star, st);
+            st.iters += it32;
             st.fallback = 1;
             return;
         }
@@ -330,6 +318,41 @@ template <> struct StarPolicy<float> {
         p_star = p;
     }
 };
+
+static __device__ __noinline__ void exact_riemann_fp64_fallback(float uL, float uR, float pL, float pR, float cL, float cR,
+                                                         double g, double eps, float& u_star, float& p_star,
+                                                         StarInfo& st)
+{
+    Gas<double> D;
+    double zeta = (g - 1.0) / (g + 1.0);
+    D.g = g;
+    D.gm1 = g - 1.0;
+    D.zeta = zeta;
+    D.mu = (g - 1.0) / (2.0 * g);
+    D.nu = (g + 1.0) / (2.0 * g);
+    D.eps = eps;
+    double us, ps;
+    exact_riemann<double>((double)uL, (double)uR, (double)pL, (double)pR, (double)cL, (double)cR, eps, 500, D, us, ps,
+                          st);
+    u_star = (float)us;
+    p_star = (float)ps;
+}
+
+template <typename R>
+__device__ __forceinline__ void q1d_waves(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S);
+
+// Non-uniform pairs: exact solver and the waves of the star state.  Out of line:
+// only a few percent of the faces of piecewise-smooth data get here, and
+// keeping it separate leaves the common (uniform-pair) path its registers.
+template <typename R>
+__device__ __noinline__ void q1d_star_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
+                                            StarInfo& st, R p_start)
+{
+    StarPolicy<R>::solve(L.u, Rr.u, L.p, Rr.p, S.c_L, S.c_R, G, p_start, S.u_star, S.p_star, st);
+    S.crw0 = st.crw0;
+    S.crw1 = st.crw1;
+    q1d_waves(L, Rr, G, S);
+}
 
 // Star state of linear_GRP_solver_Edir_Q1D (:92-134) with atc = eps:
 // uniform pairs (dist < eps) take the averaged state, all others the exact solver.
@@ -357,9 +380,7 @@ __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, co
         st.fallback = 0;
         return;
     }
-    StarPolicy<R>::solve(u_L, u_R, p_L, p_R, S.c_L, S.c_R, G, p_start, S.u_star, S.p_star, st);
-    S.crw0 = st.crw0;
-    S.crw1 = st.crw1;
+    q1d_star_exact(L, Rr, G, S, st, p_start);
 }
 
 // Waves of the star state (linear_grp_solver_Edir_Q1D.c:110-133).
@@ -389,6 +410,10 @@ __device__ __forceinline__ void q1d_waves(const Side<R>& L, const Side<R>& Rr, c
         S.speed_R = u_R + S.c_R * M<R>::sqrt_(R(0.5) * ((G.g + R(1)) * (p_star / p_R) + G.gm1) / G.g);
     }
 }
+
+template <typename R>
+__device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
+                                              R D[4], R U[4]);
 
 // Time derivatives D and t-axis values U of the quasi-1D GRP given the star
 // state: linear_grp_solver_Edir_Q1D.c:139-545 with lambda = 0.
@@ -455,6 +480,24 @@ __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, 
         D[3] = -U[1] * D_p - U[2] * T_p - U[0] * C * C * (D_u + T_v);
         return;
     }
+    q1d_derivs_exact(L, Rr, G, S, D, U);
+}
+
+// Non-acoustic case of the quasi-1D GRP (:256-547), out of line like q1d_star_exact.
+template <typename R>
+__device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
+                                              R D[4], R U[4])
+{
+    const R rho_L = L.rho, rho_R = Rr.rho;
+    const R d_rho_L = L.drho, d_rho_R = Rr.drho, t_rho_L = L.trho, t_rho_R = Rr.trho;
+    const R u_L = L.u, u_R = Rr.u, d_u_L = L.du, d_u_R = Rr.du, t_u_L = L.tu, t_u_R = Rr.tu;
+    const R v_L = L.v, v_R = Rr.v, d_v_L = L.dv, d_v_R = Rr.dv, t_v_L = L.tv, t_v_R = Rr.tv;
+    const R p_L = L.p, p_R = Rr.p, d_p_L = L.dp, d_p_R = Rr.dp, t_p_L = L.tp, t_p_R = Rr.tp;
+    const R c_L = S.c_L, c_R = S.c_R;
+    const R u_star = S.u_star, p_star = S.p_star;
+    const R rho_star_L = S.rho_star_L, rho_star_R = S.rho_star_R, c_star_L = S.c_star_L, c_star_R = S.c_star_R;
+    const R zetaL = G.zeta, zetaR = G.zeta, gL = G.g, gR = G.g;
+    R C = R(0);
 
     // non-acoustic case (:256-547)
     if (S.speed_L > R(0)) {

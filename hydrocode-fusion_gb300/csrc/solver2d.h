@@ -60,6 +60,11 @@ public:
     // (rho,u,v,p,E) each into snap_out[nt] (host memory, may be null).
     virtual int run(const RunConfig& rc, int split, int stats, const double* time_plot, int N_plot, int N_T,
                     double** snap_out, hydro_run_info* info, int* final_nt) = 0;
+    virtual int num_variants() const = 0;
+    virtual int set_variant(int v) = 0;
+    virtual int get_variant() const = 0;
+    virtual void variant_shape(int v, int* shape) const = 0;
+    virtual int autotune(const RunConfig& rc, int steps, float* times_ms) = 0;
     int m = 0, n = 0, form = 0;
 };
 

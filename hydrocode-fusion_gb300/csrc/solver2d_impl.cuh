@@ -12,6 +12,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <stdlib.h>
+
 #include <vector>
 
 #include "solver2d.h"
@@ -19,14 +21,40 @@
 
 namespace hydro {
 
-// Tile shapes of the fused kernels.
-template <typename R> struct Tiles;
-template <> struct Tiles<double> {
-    static constexpr int TJ = 16, TI = 16, NT = 256;       // unsplit step
-    static constexpr int SJ = 16, SI = 32, SNT = 256;      // split sweeps
+// Compiled configurations of the unsplit step kernel (tile TJ x TI cells,
+// NT threads, at least MINB resident CTAs per SM requested from ptxas).  The
+// autotuner (Solver2D::autotune) times them on the actual problem.
+template <typename R>
+struct StepVariant {
+    int TJ, TI, NT, MINB;
+    size_t smem;
+    const void* kern;
 };
-template <> struct Tiles<float> {
-    static constexpr int TJ = 16, TI = 32, NT = 512;
+
+template <typename R, int TJ, int TI, int NT, int MINB>
+StepVariant<R> step_variant()
+{
+    return StepVariant<R>{TJ, TI, NT, MINB, UnsplitSmem<R, TJ, TI>::bytes,
+                          (const void*)k_step_unsplit<R, TJ, TI, NT, MINB>};
+}
+
+template <typename R> struct Variants;
+template <> struct Variants<double> {
+    static std::vector<StepVariant<double>> all()
+    {
+        return {step_variant<double, 16, 16, 256, 1>(), step_variant<double, 16, 16, 256, 3>(),
+                step_variant<double, 8, 16, 128, 4>(), step_variant<double, 32, 16, 512, 1>()};
+    }
+    static constexpr int SJ = 16, SI = 32, SNT = 256;  // split sweeps
+};
+template <> struct Variants<float> {
+    static std::vector<StepVariant<float>> all()
+    {
+        return {step_variant<float, 16, 32, 512, 1>(), step_variant<float, 16, 16, 256, 2>(),
+                step_variant<float, 16, 16, 256, 3>(), step_variant<float, 16, 16, 256, 4>(),
+                step_variant<float, 8, 32, 256, 3>(),  step_variant<float, 32, 32, 512, 1>(),
+                step_variant<float, 16, 32, 512, 2>()};
+    }
     static constexpr int SJ = 16, SI = 32, SNT = 256;
 };
 
@@ -165,19 +193,25 @@ public:
         if (!cuda_ok(cudaMalloc(&ctl, sizeof(Ctl)), "control block")) return -1;
         if (!cuda_ok(cudaMalloc(&stage, sizeof(double) * 5 * (size_t)m * n), "staging")) return -1;
         if (!cuda_ok(cudaMalloc(&red, sizeof(unsigned long long)), "reduction")) return -1;
-        using TS = Tiles<R>;
-        size_t smem_u = UnsplitSmem<R, TS::TJ, TS::TI>::bytes;
+        using TS = Variants<R>;
+        variants = TS::all();
+        for (auto& v : variants)
+            if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem),
+                         "smem attr"))
+                return -1;
         size_t smem_x = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SJ, TS::SI);
         size_t smem_y = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SI, TS::SJ);
-        if (!cuda_ok(cudaFuncSetAttribute(k_step_unsplit<R, TS::TJ, TS::TI, TS::NT>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_u), "smem attr"))
-            return -1;
         if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x), "smem attr"))
             return -1;
         if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y), "smem attr"))
             return -1;
+        if (const char* e = getenv("HYDRO_STEP_VARIANT")) {
+            int v = atoi(e);
+            if (v >= 0 && v < (int)variants.size())
+                variant = v;
+        }
         return 0;
     }
 
@@ -265,6 +299,69 @@ public:
     }
 
     int cur_w = 0, cur_s = 0, cur_t = 0;
+    std::vector<StepVariant<R>> variants;
+    int variant = 0;
+
+    int num_variants() const override { return (int)variants.size(); }
+    int set_variant(int v) override
+    {
+        if (v < 0 || v >= (int)variants.size()) {
+            set_error("no such kernel variant");
+            return -1;
+        }
+        variant = v;
+        return 0;
+    }
+    int get_variant() const override { return variant; }
+    void variant_shape(int v, int* shape) const override
+    {
+        const StepVariant<R>& s = variants[v];
+        shape[0] = s.TJ;
+        shape[1] = s.TI;
+        shape[2] = s.NT;
+        shape[3] = s.MINB;
+    }
+
+    // Times every variant on `steps` steps of the uploaded state (restored
+    // afterwards) and keeps the fastest.  Returns its index.
+    int autotune(const RunConfig& rc, int steps, float* times_ms) override
+    {
+        size_t bytes = sizeof(R) * 5 * plane;
+        R* backup = nullptr;
+        if (!cuda_ok(cudaMalloc(&backup, bytes), "autotune backup")) return -1;
+        int w0 = cur_w;
+        cudaMemcpyAsync(backup, W(w0), bytes, cudaMemcpyDeviceToDevice, stream);
+        RunConfig r2 = rc;
+        r2.N = steps;
+        r2.t_all = INFINITY;
+        double tp[2] = {0.0, INFINITY};
+        int best = 0;
+        float best_ms = 1e30f;
+        for (int v = 0; v < (int)variants.size(); ++v) {
+            variant = v;
+            cudaMemcpyAsync(W(w0), backup, bytes, cudaMemcpyDeviceToDevice, stream);
+            cur_w = w0;
+            hydro_run_info info;
+            int nt;
+            if (run(r2, 0, 0, tp, 2, 2, nullptr, &info, &nt)) {
+                cudaFree(backup);
+                return -1;
+            }
+            float ms = (float)info.gpu_ms;
+            if (times_ms)
+                times_ms[v] = ms;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = v;
+            }
+        }
+        cudaMemcpyAsync(W(w0), backup, bytes, cudaMemcpyDeviceToDevice, stream);
+        cur_w = w0;
+        cudaStreamSynchronize(stream);
+        cudaFree(backup);
+        variant = best;
+        return best;
+    }
 
     void fill_gas(Gas<R>& G, double g, double eps)
     {
@@ -330,10 +427,10 @@ public:
         a.ctl = ctl;
         a.stats = stats;
 
-        using TS = Tiles<R>;
-        dim3 gu((n + TS::TI - 1) / TS::TI, (m + TS::TJ - 1) / TS::TJ);
+        using TS = Variants<R>;
+        const StepVariant<R>& V = variants[variant];
+        dim3 gu((n + V.TI - 1) / V.TI, (m + V.TJ - 1) / V.TJ);
         dim3 gs((n + TS::SI - 1) / TS::SI, (m + TS::SJ - 1) / TS::SJ);
-        size_t smem_u = UnsplitSmem<R, TS::TJ, TS::TI>::bytes;
         size_t smem_x = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SJ, TS::SI);
         size_t smem_y = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SI, TS::SJ);
 
@@ -373,7 +470,9 @@ public:
             if (r.dir == 0) {
                 a.src_s = Sx(s); a.dst_s = Sx(s ^ 1);
                 a.src_t = Ty(t); a.dst_t = Ty(t ^ 1);
-                k_step_unsplit<R, TS::TJ, TS::TI, TS::NT><<<gu, TS::NT, smem_u, stream>>>(a);
+                void* args[] = {(void*)&a};
+                if (!cuda_ok(cudaLaunchKernel(V.kern, gu, dim3(V.NT), args, V.smem, stream), "step launch"))
+                    return -1;
                 s ^= 1;
                 t ^= 1;
             } else if (r.dir == 1) {

@@ -212,7 +212,6 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
     Star<R> S;
     StarInfo st;
     q1d_star(L, Rr, a.G, S, st);
-    q1d_waves(L, Rr, a.G, S);
     R D[4], U[4];
     q1d_derivs(L, Rr, a.G, S, D, U);
     if (star_dire_check2(U, D, a.G.eps))
@@ -236,8 +235,8 @@ struct UnsplitSmem {
     static constexpr size_t bytes = sizeof(R) * (size_t)(nW + nS + nFX + nFY);
 };
 
-template <typename R, int TJ, int TI, int NT>
-__global__ void __launch_bounds__(NT) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
+template <typename R, int TJ, int TI, int NT, int MINB = 1>
+__global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
 {
     using SM = UnsplitSmem<R, TJ, TI>;
     if (halt_prologue(a.ctl, a.seq))

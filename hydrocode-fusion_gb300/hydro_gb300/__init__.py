@@ -71,6 +71,10 @@ def lib() -> ctypes.CDLL:
     L.hydro2d_download.restype = ctypes.c_int
     L.hydro2d_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(RunInfo)]
     L.hydro2d_run.restype = ctypes.c_int
+    L.hydro2d_num_variants.argtypes = [ctypes.c_void_p]
+    L.hydro2d_set_variant.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.hydro2d_get_variant.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    L.hydro2d_autotune.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     L.hydro_gb300_last_error.restype = ctypes.c_char_p
     L.hydro_gb300_kernel_launches.restype = ctypes.c_ulonglong
     _lib = L
@@ -150,6 +154,29 @@ class Solver2D:
         if lib().hydro2d_download(self._h, *out) != 0:
             raise RuntimeError("download failed: " + last_error())
         return dict(zip(("rho", "u", "v", "p", "E"), out))
+
+    def num_variants(self) -> int:
+        return int(lib().hydro2d_num_variants(self._h))
+
+    def set_variant(self, v: int):
+        if lib().hydro2d_set_variant(self._h, int(v)) != 0:
+            raise RuntimeError(last_error())
+
+    def variant(self):
+        shape = (ctypes.c_int * 4)()
+        v = lib().hydro2d_get_variant(self._h, shape)
+        return int(v), {"tile_x": shape[0], "tile_y": shape[1], "threads": shape[2], "min_ctas_per_sm": shape[3]}
+
+    def autotune(self, cfg, steps=3):
+        """Time every kernel variant on `steps` steps of the uploaded state (restored
+        afterwards); keep the fastest. Returns (best index, per-variant ms)."""
+        cfg = np.ascontiguousarray(cfg, np.float64)
+        nv = self.num_variants()
+        times = (ctypes.c_float * nv)()
+        best = lib().hydro2d_autotune(self._h, cfg, len(cfg), int(steps), times)
+        if best < 0:
+            raise RuntimeError("autotune failed: " + last_error())
+        return int(best), [float(t) for t in times]
 
     def run(self, cfg, split=False, stats=False) -> RunInfo:
         cfg = np.ascontiguousarray(cfg, np.float64)

@@ -109,11 +109,21 @@ int hydro2d_download(hydro2d_t *h, double *rho, double *u, double *v, double *p,
  * uploaded state: split = 0 unsplit, 1 dimension split.  stats != 0 counts
  * Newton faces/iterations. */
 int hydro2d_run(hydro2d_t *h, const double *cfg, int ncfg, int split, int stats, hydro_run_info *info);
-/* 1D run (order 1 = Godunov, 2 = GRP) of an m-cell tube held in host arrays
- * (final state written back; E may be NULL, then the driver's formula is used),
- * configured by cfg[] like the 1D scheme entry points, with no plot snapshots. */
+/* 1D run (order 1 = Godunov, 2 = GRP) of an m-cell tube held in host arrays,
+ * configured by cfg[] like the 1D scheme entry points, with no plot snapshots.
+ * rho, u, p (and E) hold the initial state and receive the final one; E is the
+ * initial specific total energy, or NULL to use the 1D driver's formula. */
 int hydro1d_run(int m, double *rho, double *u, double *p, double *E, const double *cfg, int ncfg, int order,
                 hydro_run_info *info);
+/* Kernel variants of the unsplit step (tile shape / threads / occupancy).
+ * hydro2d_get_variant fills shape[4] = {tile x, tile y, threads, min CTAs per SM}. */
+int hydro2d_num_variants(hydro2d_t *h);
+int hydro2d_set_variant(hydro2d_t *h, int v);
+int hydro2d_get_variant(hydro2d_t *h, int *shape);
+/* Autotuner: times every variant on `steps` steps of the uploaded state (which
+ * is restored), keeps the fastest and returns its index; times_ms (may be
+ * NULL) receives one time per variant. */
+int hydro2d_autotune(hydro2d_t *h, const double *cfg, int ncfg, int steps, float *times_ms);
 /* Number of CUDA kernels launched by this library since load (all solvers). */
 unsigned long long hydro_gb300_kernel_launches(void);
 /* Message of the last failing call in this thread ("" if none). */

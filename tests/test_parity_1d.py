@@ -16,7 +16,8 @@ def _run(hg, rho, u, p, cfg, order):
     L = hg.lib()
     L.hydro1d_run.restype = ctypes.c_int
     rho, u, p = (np.array(a, np.float64) for a in (rho, u, p))
-    E = np.zeros_like(rho)
+    g = float(cfg[6])
+    E = 0.5 * u * u + p / (g - 1.0) / rho  # the 1D driver's energy (src/hydrocode_1D/hydrocode.c:235)
     info = hg.RunInfo()
     cfg = np.ascontiguousarray(cfg, np.float64)
     P = ctypes.POINTER(ctypes.c_double)
