@@ -332,12 +332,10 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
 
 // Runs one 1D problem.  state: [4][m] rho,u,p,E in (CV.*[0]) and the final
 // state out; snaps: [n_plot][4][m] host snapshot slots (may be null when n_plot == 2).
-static int run1d(int m, int order, const double* cfg, int ncfg, double* state, const double* time_plot, int n_plot,
-                 double* snaps_host, hydro_run_info* info, int* nt_out)
+// Fills the kernel arguments from config[] semantics; -2 for an unknown boundary code.
+static int prepare_args(Run1DArgs& a, int m, int order, const double* cfg, int ncfg, int n_plot)
 {
-    memset(info, 0, sizeof(*info));
     auto at = [&](int k) { return k < ncfg ? cfg[k] : INFINITY; };
-    Run1DArgs a;
     memset(&a, 0, sizeof(a));
     a.m = m;
     a.order = order;
@@ -366,7 +364,30 @@ static int run1d(int m, int order, const double* cfg, int ncfg, double* state, c
     G.g_g1 = g / (g - 1.0); G.inv_g = 1.0 / g; G.cexp = 0.5 * (g - 1.0) / g; G.sexp = 2.0 * g / (g - 1.0);
     G.e1 = 0.5 / zeta; G.e2 = (1.0 + zeta) / zeta; G.opz = 1.0 + zeta; G.op2z = 1.0 + 2.0 * zeta;
     G.eps = a.eps; G.g64 = g; G.eps64 = a.eps;
+    return 0;
+}
 
+static void info_from(const double o[8], hydro_run_info* info)
+{
+    info->k_out = (int)o[0];
+    info->time = o[2];
+    info->tau = o[3];
+    info->halted = (int)o[4];
+    info->newton_faces = (unsigned long long)o[5];
+    info->newton_iters = (unsigned long long)o[6];
+    info->sweeps_launched = 1;
+}
+
+// Runs one 1D problem.  state: [4][m] rho,u,p,E in (CV.*[0]) and the final
+// state out; snaps: [n_plot][4][m] host snapshot slots (may be null when n_plot == 2).
+static int run1d(int m, int order, const double* cfg, int ncfg, double* state, const double* time_plot, int n_plot,
+                 double* snaps_host, hydro_run_info* info, int* nt_out)
+{
+    memset(info, 0, sizeof(*info));
+    Run1DArgs a;
+    int prc = prepare_args(a, m, order, cfg, ncfg, n_plot);
+    if (prc)
+        return prc;
     size_t need = 4 * (size_t)m * 2 + (size_t)n_plot * 4 * m + n_plot + 3 * (size_t)m + 9 * (size_t)(m + 1) + 8;
     double* mem = nullptr;
     if (!cuda_ok(cudaMalloc(&mem, need * sizeof(double)), "1D buffers")) return -1;
@@ -417,14 +438,8 @@ static int run1d(int m, int order, const double* cfg, int ncfg, double* state, c
     cudaFree(mem);
     if (rc)
         return rc;
-    info->k_out = (int)o[0];
-    info->time = o[2];
-    info->tau = o[3];
-    info->halted = (int)o[4];
-    info->newton_faces = (unsigned long long)o[5];
-    info->newton_iters = (unsigned long long)o[6];
+    info_from(o, info);
     info->gpu_ms = ms;
-    info->sweeps_launched = 1;
     *nt_out = nt;
     return 0;
 }
