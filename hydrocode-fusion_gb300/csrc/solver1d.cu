@@ -444,6 +444,101 @@ static int run1d(int m, int order, const double* cfg, int ncfg, double* state, c
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the 1D run.
+//
+// Some callers cannot allocate device memory: code that runs while a stream
+// is being captured into a CUDA graph (cudaMalloc is not allowed there),
+// frameworks that own the whole device pool through their own allocator, or
+// embedded drivers whose memory budget is fixed at start-up.  For them the
+// scratch of the 1D kernel (copy of the initial state, one snapshot slot,
+// slopes, interface values, time derivatives, fluxes, result words) lives in
+// the file-scope array below, sized for at most HYDRO1D_NOALLOC_MAX_CELLS
+// cells: 20*m + 19 doubles, 2.6 MB at the limit, held by every GPU that loads
+// the library until the process exits.
+//
+// Host code cannot use the array's name as a device address (it names a
+// host-side stand-in), so the device address is looked up with
+// cudaGetSymbolAddress once per device, on the first call made on that device
+// with that device current; that first call should therefore come before any
+// stream capture.  Every call shares the one array and it keeps the previous
+// call's contents: the slopes and result words are cleared on each call, and
+// calls that overlap on the GPU (several streams, several host threads) race
+// on it, so a caller must serialise them.
+// ---------------------------------------------------------------------------
+#define HYDRO1D_NOALLOC_MAX_CELLS 16384
+#define HYDRO1D_NOALLOC_DOUBLES (20 * HYDRO1D_NOALLOC_MAX_CELLS + 19)
+
+static __device__ __align__(256) double g_noalloc_scratch[HYDRO1D_NOALLOC_DOUBLES];
+
+static double* noalloc_scratch_address(int* err)
+{
+    enum { MAX_DEVICES = 64 };
+    static double* addr[MAX_DEVICES];
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice") || dev < 0 || dev >= MAX_DEVICES) {
+        *err = -1;
+        return nullptr;
+    }
+    if (!addr[dev]) {
+        void* p = nullptr;
+        if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress")) {
+            *err = -1;
+            return nullptr;
+        }
+        addr[dev] = (double*)p;
+    }
+    return addr[dev];
+}
+
+static int run1d_noalloc(int m, double* d_state, const double* cfg, int ncfg, int order, cudaStream_t st,
+                         hydro_run_info* info)
+{
+    memset(info, 0, sizeof(*info));
+    if (m < 2 || m > HYDRO1D_NOALLOC_MAX_CELLS) {
+        set_error("hydro1d_run_noalloc: m must be in [2, 16384] (fixed device scratch)");
+        return -3;
+    }
+    if (!d_state) {
+        set_error("hydro1d_run_noalloc: null state");
+        return -3;
+    }
+    Run1DArgs a;
+    int prc = prepare_args(a, m, order, cfg, ncfg, 2);
+    if (prc)
+        return prc;
+    int err = 0;
+    double* base = noalloc_scratch_address(&err);
+    if (!base)
+        return err;
+    double* init = base;
+    double* snaps = init + 4 * (size_t)m;
+    double* tp = snaps + 4 * (size_t)m;
+    double* s = tp + 2;
+    double* mid = s + 3 * (size_t)m;
+    double* dire = mid + 3 * (size_t)(m + 1);
+    double* F = dire + 3 * (size_t)(m + 1);
+    double* out = F + 3 * (size_t)(m + 1);
+    double tph[2] = {0.0, a.t_all};
+    if (!cuda_ok(cudaMemcpyAsync(init, d_state, 4 * m * sizeof(double), cudaMemcpyDeviceToDevice, st), "noalloc copy") ||
+        !cuda_ok(cudaMemcpyAsync(tp, tph, 2 * sizeof(double), cudaMemcpyHostToDevice, st), "noalloc copy") ||
+        !cuda_ok(cudaMemsetAsync(s, 0, 3 * m * sizeof(double), st), "noalloc clear") ||
+        !cuda_ok(cudaMemsetAsync(out, 0, 8 * sizeof(double), st), "noalloc clear"))
+        return -1;
+    a.init = init; a.cur = d_state; a.snaps = snaps; a.time_plot = tp; a.s = s; a.mid = mid; a.dire = dire; a.F = F;
+    a.out = out;
+    k_run1d<<<1, 512, 0, st>>>(a);
+    count_launch();
+    if (!cuda_ok(cudaGetLastError(), "noalloc launch"))
+        return -1;
+    double o[8];
+    if (!cuda_ok(cudaMemcpyAsync(o, out, 8 * sizeof(double), cudaMemcpyDeviceToHost, st), "noalloc result") ||
+        !cuda_ok(cudaStreamSynchronize(st), "noalloc run"))
+        return -1;
+    info_from(o, info);
+    return 0;
+}
+
 static void entry_1d(const int m, struct cell_var_stru CV, double* cpu_time, int* N_plot, double time_plot[], int order)
 {
     std::vector<double> state(4 * (size_t)m);
@@ -507,6 +602,12 @@ void Godunov_solver_EUL_source(const int m, struct cell_var_stru CV, double* cpu
 void GRP_solver_EUL_source(const int m, struct cell_var_stru CV, double* cpu_time, int* N_plot, double time_plot[])
 {
     entry_1d(m, CV, cpu_time, N_plot, time_plot, 2);
+}
+
+int hydro1d_run_noalloc(int m, double* d_state, const double* cfg, int ncfg, int order, void* stream,
+                        hydro_run_info* info)
+{
+    return run1d_noalloc(m, d_state, cfg, ncfg, order, (cudaStream_t)stream, info);
 }
 
 int hydro1d_run(int m, double* rho, double* u, double* p, double* E, const double* cfg, int ncfg, int order,
