@@ -171,17 +171,10 @@ def main():
     s.close()
 
     # FP64 parity form, same grid
-    s64 = hg.Solver2D(m, n, hg.FORM_FP64)
-    s64.upload(rho, u, v, p)
-    tune64 = None
-    if not args.no_tune and args.fp64_steps > 0:
-        best64, times64 = s64.autotune(hg.config_2d(t_all=-1, steps=2, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), steps=2)
-        tune64 = {"best": best64, "ms_per_2_steps": times64}
-    s64.run(hg.config_2d(t_all=-1, steps=3, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4))
-    s64.upload(rho, u, v, p)
-    i64 = s64.run(hg.config_2d(t_all=-1, steps=args.fp64_steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), stats=True)
-    fp64_rate = m * n * args.fp64_steps / (i64.gpu_ms * 1e-3)
-    s64.close()
+    fp64 = None
+    if args.fp64_steps > 0:
+        fp64 = fp64_run(hg, m, n, rho, u, v, p, args)
+    line_fp64 = fp64
 
     peak, peak_kind = peaks()
     alg_bytes = 96.0 * m * n  # per launch: 12 FP32 fields read + written
@@ -201,14 +194,28 @@ def main():
             "config": {"workload": workload, "form": "fp32", "grid": [m, n], "l2": "inputs larger than L2 (13 planes x 4 B x 16.8M cells)",
                        "kernel_variant": variant, "autotune": tune},
             "roofline": roof, "cpu_baseline": cpu, "gpu_launches": int(launches),
-            "fp64": {"value": fp64_rate, "unit": "cell-updates/s", "steps": args.fp64_steps,
-                     "ms_per_step": i64.gpu_ms / args.fp64_steps,
-                     "newton_faces_per_step": i64.newton_faces / args.fp64_steps,
-                     "newton_iters_per_face": (i64.newton_iters / i64.newton_faces) if i64.newton_faces else 0.0,
-                     "autotune": tune64},
-            "clocks": cs.summary()}
+            "fp64": line_fp64, "clocks": cs.summary()}
     if rank == 0:
         print(json.dumps(line))
+
+
+def fp64_run(hg, m, n, rho, u, v, p, args):
+    s64 = hg.Solver2D(m, n, hg.FORM_FP64)
+    s64.upload(rho, u, v, p)
+    tune64 = None
+    if not args.no_tune and args.fp64_steps > 0:
+        best64, times64 = s64.autotune(hg.config_2d(t_all=-1, steps=2, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), steps=2)
+        tune64 = {"best": best64, "ms_per_2_steps": times64}
+    s64.run(hg.config_2d(t_all=-1, steps=3, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4))
+    s64.upload(rho, u, v, p)
+    i64 = s64.run(hg.config_2d(t_all=-1, steps=args.fp64_steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), stats=True)
+    fp64_rate = m * n * args.fp64_steps / (i64.gpu_ms * 1e-3)
+    s64.close()
+    return {"value": fp64_rate, "unit": "cell-updates/s", "steps": args.fp64_steps,
+            "ms_per_step": i64.gpu_ms / args.fp64_steps,
+            "newton_faces_per_step": i64.newton_faces / args.fp64_steps,
+            "newton_iters_per_face": (i64.newton_iters / i64.newton_faces) if i64.newton_faces else 0.0,
+            "autotune": tune64}
 
 
 if __name__ == "__main__":

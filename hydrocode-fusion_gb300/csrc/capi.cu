@@ -294,6 +294,8 @@ int hydro2d_get_variant(hydro2d_t* h, int* shape)
         h->s->variant_shape(v, shape);
     return v;
 }
+int hydro2d_set_mlp(hydro2d_t* h, const float* params) { return h->s->set_mlp(params); }
+
 int hydro2d_autotune(hydro2d_t* h, const double* cfg, int ncfg, int steps, float* times_ms)
 {
     return h->s->autotune(run_config_from(cfg, ncfg), steps, times_ms);

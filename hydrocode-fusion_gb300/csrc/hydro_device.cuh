@@ -26,12 +26,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "hydro_pow.cuh"
+
 namespace hydro {
 
 template <typename R> struct M;
 template <> struct M<double> {
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-    static __device__ __forceinline__ double pow_(double x, double y) { return pow(x, y); }
+    // double-double pow: agrees with a correctly rounded pow (hydro_pow.cuh)
+    static __device__ __forceinline__ double pow_(double x, double y) { return dd_pow(x, y); }
     static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
     static __device__ __forceinline__ bool finite_(double x)
     {
@@ -695,8 +698,9 @@ struct FaceOut {
 // Assemble the GRP_2D_flux outputs (flux_solver.c:195-220) of an axis-aligned
 // face from the normal-frame t-axis values U and derivatives D.  YDIR: the
 // normal is +y, so the x-velocity is minus the tangential velocity.
-template <typename R, bool YDIR>
-__device__ __forceinline__ void face_flux(const R D[4], const R U[4], R tau, R htau, const Gas<R>& G, FaceOut<R>& o)
+template <typename R>
+__device__ __forceinline__ void face_flux(const R D[4], const R U[4], R tau, R htau, const Gas<R>& G, FaceOut<R>& o,
+                                          bool YDIR)
 {
     R rho_mid = U[0] + htau * D[0];
     R a = U[1] + htau * D[1];  // normal velocity at t + tau/2

@@ -65,6 +65,7 @@ public:
     virtual int get_variant() const = 0;
     virtual void variant_shape(int v, int* shape) const = 0;
     virtual int autotune(const RunConfig& rc, int steps, float* times_ms) = 0;
+    virtual int set_mlp(const float* params) = 0;
     int m = 0, n = 0, form = 0;
 };
 

@@ -31,16 +31,17 @@ struct StepVariant {
     const void* kern;
 };
 
-template <typename R, int TJ, int TI, int NT, int MINB>
+template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false>
 StepVariant<R> step_variant()
 {
-    return StepVariant<R>{TJ, TI, NT, MINB, UnsplitSmem<R, TJ, TI>::bytes,
-                          (const void*)k_step_unsplit<R, TJ, TI, NT, MINB>};
+    return StepVariant<R>{TJ, TI, NT, MINB,
+                          LEARNED ? UnsplitSmem<R, TJ, TI>::bytes_learned : UnsplitSmem<R, TJ, TI>::bytes,
+                          (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED>};
 }
 
 template <typename R> struct Variants;
 template <> struct Variants<double> {
-    static std::vector<StepVariant<double>> all()
+    static std::vector<StepVariant<double>> all(bool)
     {
         return {step_variant<double, 16, 16, 256, 1>(), step_variant<double, 16, 16, 256, 3>(),
                 step_variant<double, 8, 16, 128, 4>(), step_variant<double, 32, 16, 512, 1>()};
@@ -48,8 +49,11 @@ template <> struct Variants<double> {
     static constexpr int SJ = 16, SI = 32, SNT = 256;  // split sweeps
 };
 template <> struct Variants<float> {
-    static std::vector<StepVariant<float>> all()
+    static std::vector<StepVariant<float>> all(bool learned)
     {
+        if (learned)
+            return {step_variant<float, 32, 32, 512, 1, true>(), step_variant<float, 16, 32, 512, 1, true>(),
+                    step_variant<float, 16, 16, 256, 2, true>()};
         return {step_variant<float, 16, 32, 512, 1>(), step_variant<float, 16, 16, 256, 2>(),
                 step_variant<float, 16, 16, 256, 3>(), step_variant<float, 16, 16, 256, 4>(),
                 step_variant<float, 8, 32, 256, 3>(),  step_variant<float, 32, 32, 512, 1>(),
@@ -194,11 +198,21 @@ public:
         if (!cuda_ok(cudaMalloc(&stage, sizeof(double) * 5 * (size_t)m * n), "staging")) return -1;
         if (!cuda_ok(cudaMalloc(&red, sizeof(unsigned long long)), "reduction")) return -1;
         using TS = Variants<R>;
-        variants = TS::all();
-        for (auto& v : variants)
+        variants = TS::all(form == HYDRO_FORM_FP32_LEARNED);
+        if (form == HYDRO_FORM_FP32_LEARNED) {
+            if (!cuda_ok(cudaMalloc(&mlp_frag, sizeof(uint32_t) * MLP_NFRAG), "network") ||
+                !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network"))
+                return -1;
+        }
+        for (auto& v : variants) {
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem),
                          "smem attr"))
                 return -1;
+            // all of the unified L1/shared storage as shared memory, so several CTAs fit per SM
+            if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                         "carveout attr"))
+                return -1;
+        }
         size_t smem_x = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SJ, TS::SI);
         size_t smem_y = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SI, TS::SJ);
         if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT>,
@@ -215,9 +229,30 @@ public:
         return 0;
     }
 
+    uint32_t* mlp_frag = nullptr;
+    float* mlp_prm = nullptr;
+    bool mlp_set = false;
+
+    int set_mlp(const float* params) override
+    {
+        if (form != HYDRO_FORM_FP32_LEARNED) {
+            set_error("set_mlp: the solver is not in the learned form");
+            return -1;
+        }
+        if (!cuda_ok(cudaMemcpyAsync(mlp_prm, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice, stream),
+                     "network upload"))
+            return -1;
+        k_mlp_pack<<<(8 * 32 + 4 * 8 * 32 + 4 * 32 + 127) / 128, 128, 0, stream>>>(mlp_prm, mlp_frag);
+        count_launch();
+        mlp_set = true;
+        return cuda_ok(cudaStreamSynchronize(stream), "network pack") ? 0 : -1;
+    }
+
     ~Solver2D() override
     {
         if (stream) cudaStreamSynchronize(stream);
+        cudaFree(mlp_frag);
+        cudaFree(mlp_prm);
         cudaFree(mem);
         cudaFree(ghost0);
         cudaFree(ctl);
@@ -426,6 +461,14 @@ public:
         a.by = rc.by;
         a.ctl = ctl;
         a.stats = stats;
+        if (form == HYDRO_FORM_FP32_LEARNED) {
+            if (!mlp_set) {
+                set_error("learned form: no network weights installed (hydro2d_set_mlp)");
+                return -1;
+            }
+            a.mlp_frag = mlp_frag;
+            a.mlp_prm = mlp_prm;
+        }
 
         using TS = Variants<R>;
         const StepVariant<R>& V = variants[variant];

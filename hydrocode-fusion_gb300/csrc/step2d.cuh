@@ -30,6 +30,7 @@
 #pragma once
 
 #include "hydro_device.cuh"
+#include "learned.cuh"
 
 namespace hydro {
 
@@ -68,6 +69,8 @@ struct StepArgs {
     int seq;               // launch sequence number (1, 2, ...) of this sweep
     int split_kind;        // 0 unsplit; for split sweeps the direction is the template parameter
     int stats;             // count Newton faces / iterations
+    const uint32_t* mlp_frag;  // learned form: packed BF16 network
+    const float* mlp_prm;      // learned form: FP32 parameters (biases)
 };
 
 // ---------------------------------------------------------------------------
@@ -204,21 +207,64 @@ __device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigne
 }
 
 // Solve one face given its two sides in the face's normal frame.
-template <typename R, bool YDIR>
+template <typename R>
 __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, const StepArgs<R>& a, FaceOut<R>& o,
-                                          int& iters)
+                                          int& iters, bool ydir, R p_start = R(-1))
 {
     int code = ifvar_bad(L, Rr, a.G.eps) ? 1 : 0;
     Star<R> S;
     StarInfo st;
-    q1d_star(L, Rr, a.G, S, st);
+    q1d_star(L, Rr, a.G, S, st, p_start);
     R D[4], U[4];
     q1d_derivs(L, Rr, a.G, S, D, U);
     if (star_dire_check2(U, D, a.G.eps))
         code = 2;
-    face_flux<R, YDIR>(D, U, a.tau, a.htau, a.G, o);
+    face_flux<R>(D, U, a.tau, a.htau, a.G, o, ydir);
     iters = st.iters;
     return code;
+}
+
+// Learned starting pressure of the exact solver for every lane of the warp
+// whose face is not a uniform pair (warp-collective: all 32 lanes call it).
+// Returns -1 where no guess applies (uniform pair, inactive lane, a pair that
+// would generate vacuum, a non-finite prediction).
+__device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<float>& Rr, bool active,
+                                               const Gas<float>& G, const MlpShared& M)
+{
+    const float cL = sqrtf(G.g * L.p / L.rho), cR = sqrtf(G.g * Rr.p / Rr.rho);
+    const float dist = sqrtf((L.rho - Rr.rho) * (L.rho - Rr.rho) + (L.u - Rr.u) * (L.u - Rr.u) +
+                             (L.p - Rr.p) * (L.p - Rr.p));
+    const bool need = active && !StarPolicy<float>::uniform(dist, L.rho + Rr.rho + L.p + Rr.p + fabsf(L.u) + fabsf(Rr.u), G);
+    float pg = -1.f;
+    if (__any_sync(0xffffffffu, need)) {
+        float x[6];
+        float pbar = mlp_features(L.rho, L.u, L.p, cL, Rr.rho, Rr.u, Rr.p, cR, x);
+        if (!need)
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                x[k] = 0.f;
+        const float y = warp_mlp(x, M);
+        const bool vac = (Rr.u - L.u) >= 0.9f * 2.f * (cL + cR) / G.gm1;
+        const float p = pbar * __expf(y);
+        if (need && !vac && p > 0.f && p < INFINITY)
+            pg = p;
+    }
+    return pg;
+}
+template <typename R>
+__device__ __forceinline__ R learned_guess_any(const Side<R>& L, const Side<R>& Rr, bool active, const Gas<R>& G,
+                                               const MlpShared& M);
+template <>
+__device__ __forceinline__ float learned_guess_any<float>(const Side<float>& L, const Side<float>& Rr, bool active,
+                                                          const Gas<float>& G, const MlpShared& M)
+{
+    return learned_guess(L, Rr, active, G, M);
+}
+template <>
+__device__ __forceinline__ double learned_guess_any<double>(const Side<double>&, const Side<double>&, bool,
+                                                            const Gas<double>&, const MlpShared&)
+{
+    return -1.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -233,9 +279,11 @@ struct UnsplitSmem {
     static constexpr int nFX = 8 * (TJ + 1) * TI;
     static constexpr int nFY = 8 * TJ * (TI + 1);
     static constexpr size_t bytes = sizeof(R) * (size_t)(nW + nS + nFX + nFY);
+    // the learned form appends the network image
+    static constexpr size_t bytes_learned = (bytes + 15) / 16 * 16 + sizeof(MlpShared);
 };
 
-template <typename R, int TJ, int TI, int NT, int MINB = 1>
+template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
 __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
 {
     using SM = UnsplitSmem<R, TJ, TI>;
@@ -246,6 +294,9 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
     R* S = W + SM::nW;
     R* FX = S + SM::nS;
     R* FY = FX + SM::nFX;
+    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + (SM::bytes + 15) / 16 * 16);
+    if (LEARNED)
+        mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
     const int tid = threadIdx.x;
     const int I0 = blockIdx.x * TI, J0 = blockIdx.y * TJ;
     const int m = a.m, n = a.n, slot = a.seq % 3;
@@ -326,16 +377,22 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
     }
     __syncthreads();
 
-    // 3. faces
+    // 3. faces, in warp-uniform rounds (every lane of a warp iterates together,
+    //    so the learned form can run its warp-collective network)
     constexpr int NFX = (TJ + 1) * TI, NFY = TJ * (TI + 1);
     int my_iters = 0, my_newton = 0;
-    for (int f = tid; f < NFX + NFY; f += NT) {
-        if (f < NFX) {
-            int fj = f / TI, fi = f - fj * TI;
-            int j = J0 + fj, i = I0 + fi;
-            if (j > m || i >= n)
-                continue;
-            Side<R> L, Rr;
+    const int lane = tid & 31;
+    for (int fb = tid - lane; fb < NFX + NFY; fb += NT) {
+        const int f = fb + lane;
+        const bool ydir = f >= NFX;
+        bool active = f < NFX + NFY;
+        int lj = 0, li = 0, j = 0, i = 0;
+        Side<R> L, Rr;
+        if (active && !ydir) {
+            const int fj = f / TI, fi = f - fj * TI;
+            lj = fj; li = fi;
+            j = J0 + fj; i = I0 + fi;
+            active = !(j > m || i >= n);
             // left cell (j-1): slopes at (fj, fi+1), values at (fj+1, fi+2)
             L.drho = Sx(0, fj, fi + 1); L.du = Sx(1, fj, fi + 1); L.dv = Sx(2, fj, fi + 1); L.dp = Sx(3, fj, fi + 1);
             L.trho = Sx(4, fj, fi + 1); L.tu = Sx(5, fj, fi + 1); L.tv = Sx(6, fj, fi + 1); L.tp = Sx(7, fj, fi + 1);
@@ -349,28 +406,14 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
             Rr.u = Wx(1, fj + 2, fi + 2) - a.hhx * Rr.du;
             Rr.v = Wx(2, fj + 2, fi + 2) - a.hhx * Rr.dv;
             Rr.p = Wx(3, fj + 2, fi + 2) - a.hhx * Rr.dp;
-            FaceOut<R> o;
-            int it;
-            int code = solve_face<R, false>(L, Rr, a, o, it);
-            if (it >= 0) {
-                my_newton++;
-                my_iters += it;
-            }
-            report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                FXx(k, fj, fi) = o.F[k];
-                FXx(4 + k, fj, fi) = o.I[k];
-            }
-        } else {
-            int g = f - NFX;
-            int gj = g / (TI + 1), gi = g - gj * (TI + 1);
-            int j = J0 + gj, i = I0 + gi;
-            if (j >= m || i > n)
-                continue;
+        } else if (active) {
+            const int g = f - NFX;
+            const int gj = g / (TI + 1), gi = g - gj * (TI + 1);
+            lj = gj; li = gi;
+            j = J0 + gj; i = I0 + gi;
+            active = !(j >= m || i > n);
             // lower cell (i-1): slopes at (gj+1, gi), values at (gj+2, gi+1); rotated to the +y normal frame:
             // normal velocity v, tangential -u; normal derivatives are the y-slopes, tangential the negated x-slopes
-            Side<R> D, U;
             {
                 R t0 = Sx(4, gj + 1, gi), t1 = Sx(5, gj + 1, gi), t2 = Sx(6, gj + 1, gi), t3 = Sx(7, gj + 1, gi);
                 R s0 = Sx(0, gj + 1, gi), s1 = Sx(1, gj + 1, gi), s2 = Sx(2, gj + 1, gi), s3 = Sx(3, gj + 1, gi);
@@ -378,9 +421,9 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
                 R uu = Wx(1, gj + 2, gi + 1) + a.hhy * t1;
                 R vv = Wx(2, gj + 2, gi + 1) + a.hhy * t2;
                 R pp = Wx(3, gj + 2, gi + 1) + a.hhy * t3;
-                D.rho = rr; D.u = vv; D.v = -uu; D.p = pp;
-                D.drho = t0; D.du = t2; D.dv = -t1; D.dp = t3;
-                D.trho = -s0; D.tu = -s2; D.tv = s1; D.tp = -s3;
+                L.rho = rr; L.u = vv; L.v = -uu; L.p = pp;
+                L.drho = t0; L.du = t2; L.dv = -t1; L.dp = t3;
+                L.trho = -s0; L.tu = -s2; L.tv = s1; L.tp = -s3;
             }
             {
                 R t0 = Sx(4, gj + 1, gi + 1), t1 = Sx(5, gj + 1, gi + 1), t2 = Sx(6, gj + 1, gi + 1), t3 = Sx(7, gj + 1, gi + 1);
@@ -389,22 +432,36 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
                 R uu = Wx(1, gj + 2, gi + 2) - a.hhy * t1;
                 R vv = Wx(2, gj + 2, gi + 2) - a.hhy * t2;
                 R pp = Wx(3, gj + 2, gi + 2) - a.hhy * t3;
-                U.rho = rr; U.u = vv; U.v = -uu; U.p = pp;
-                U.drho = t0; U.du = t2; U.dv = -t1; U.dp = t3;
-                U.trho = -s0; U.tu = -s2; U.tv = s1; U.tp = -s3;
+                Rr.rho = rr; Rr.u = vv; Rr.v = -uu; Rr.p = pp;
+                Rr.drho = t0; Rr.du = t2; Rr.dv = -t1; Rr.dp = t3;
+                Rr.trho = -s0; Rr.tu = -s2; Rr.tv = s1; Rr.tp = -s3;
             }
-            FaceOut<R> o;
-            int it;
-            int code = solve_face<R, true>(D, U, a, o, it);
-            if (it >= 0) {
-                my_newton++;
-                my_iters += it;
+        }
+        R p_start = R(-1);
+        if (LEARNED)
+            p_start = learned_guess_any<R>(L, Rr, active, a.G, Mlp);
+        if (!active)
+            continue;
+        FaceOut<R> o;
+        int it;
+        const int code = solve_face<R>(L, Rr, a, o, it, ydir, p_start);
+        if (it >= 0) {
+            my_newton++;
+            my_iters += it;
+        }
+        if (!ydir) {
+            report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                FXx(k, lj, li) = o.F[k];
+                FXx(4 + k, lj, li) = o.I[k];
             }
+        } else {
             report_face(a.ctl, slot, 1, (unsigned long long)j * (n + 1) + i, code);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                FYx(k, gj, gi) = o.F[k];
-                FYx(4 + k, gj, gi) = o.I[k];
+                FYx(k, lj, li) = o.F[k];
+                FYx(4 + k, lj, li) = o.I[k];
             }
         }
     }
@@ -573,11 +630,8 @@ __global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R
         L.trho = L.tu = L.tv = L.tp = R(0);
         Rr.trho = Rr.tu = Rr.tv = Rr.tp = R(0);
         FaceOut<R> o;
-        int it, code;
-        if (YDIR)
-            code = solve_face<R, true>(L, Rr, a, o, it);
-        else
-            code = solve_face<R, false>(L, Rr, a, o, it);
+        int it;
+        const int code = solve_face<R>(L, Rr, a, o, it, YDIR != 0);
         if (it >= 0) {
             my_newton++;
             my_iters += it;

@@ -23,6 +23,9 @@ FORM_FP32 = 1
 FORM_FP32_LEARNED = 2
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_fp = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+MLP_NPARAM = 4673
+WEIGHTS_PATH = os.path.join(PKG_DIR, "weights", "riemann_guess_6_64_64_1.f32")
 
 
 class RunInfo(ctypes.Structure):
@@ -75,6 +78,19 @@ def lib() -> ctypes.CDLL:
     L.hydro2d_set_variant.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.hydro2d_get_variant.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.hydro2d_autotune.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    L.hydro2d_set_mlp.argtypes = [ctypes.c_void_p, _fp]
+    vp = ctypes.c_void_p
+    L.hydro_mlp_create.argtypes = [ctypes.POINTER(vp), ctypes.c_ulonglong]
+    L.hydro_mlp_destroy.argtypes = [vp]
+    L.hydro_mlp_destroy.restype = None
+    L.hydro_mlp_get_params.argtypes = [vp, _fp]
+    L.hydro_mlp_set_params.argtypes = [vp, _fp]
+    L.hydro_mlp_generate.argtypes = [vp, ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_void_p]
+    L.hydro_mlp_get_data.argtypes = [vp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]
+    L.hydro_mlp_train.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_longlong, ctypes.c_void_p]
+    L.hydro_mlp_gradient.argtypes = [vp, _fp, _fp, ctypes.c_int, _fp, ctypes.POINTER(ctypes.c_float)]
+    L.hydro_mlp_predict.argtypes = [vp, _fp, ctypes.c_int, _fp]
+    L.hydro_mlp_features.argtypes = [_dp, ctypes.c_int, ctypes.c_double, _fp]
     L.hydro_gb300_last_error.restype = ctypes.c_char_p
     L.hydro_gb300_kernel_launches.restype = ctypes.c_ulonglong
     _lib = L
@@ -178,6 +194,10 @@ class Solver2D:
             raise RuntimeError("autotune failed: " + last_error())
         return int(best), [float(t) for t in times]
 
+    def set_mlp(self, params):
+        if lib().hydro2d_set_mlp(self._h, np.ascontiguousarray(params, np.float32)) != 0:
+            raise RuntimeError(last_error())
+
     def run(self, cfg, split=False, stats=False) -> RunInfo:
         cfg = np.ascontiguousarray(cfg, np.float64)
         info = RunInfo()
@@ -186,13 +206,98 @@ class Solver2D:
         return info
 
 
-def run_2d(rho, u, v, p, cfg, split=False, form=FORM_FP64, stats=False):
-    """Upload, run, download; returns (state dict, RunInfo)."""
+def run_2d(rho, u, v, p, cfg, split=False, form=FORM_FP64, stats=False, mlp=None):
+    """Upload, run, download; returns (state dict, RunInfo).  The learned form
+    uses `mlp` (a parameter vector) or the shipped trained weights."""
     m, n = np.shape(rho)
     s = Solver2D(m, n, form)
     try:
+        if form == FORM_FP32_LEARNED:
+            s.set_mlp(load_weights() if mlp is None else mlp)
         s.upload(rho, u, v, p, None, float(cfg[6]))
         info = s.run(cfg, split=split, stats=stats)
         return s.download(), info
     finally:
         s.close()
+
+
+class Mlp:
+    """The learned Newton starting pressure network (hydro_mlp_* in the C ABI)."""
+
+    def __init__(self, seed: int = 1):
+        h = ctypes.c_void_p()
+        if lib().hydro_mlp_create(ctypes.byref(h), seed) != 0:
+            raise RuntimeError("hydro_mlp_create failed: " + last_error())
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().hydro_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(MLP_NPARAM, np.float32)
+        if lib().hydro_mlp_get_params(self._h, p) != 0:
+            raise RuntimeError(last_error())
+        return p
+
+    def set_params(self, p):
+        if lib().hydro_mlp_set_params(self._h, np.ascontiguousarray(p, np.float32)) != 0:
+            raise RuntimeError(last_error())
+
+    def generate(self, n: int, seed: int = 7, gamma: float = 1.4, want_raw: bool = False):
+        raw = np.zeros((n, 6)) if want_raw else None
+        if lib().hydro_mlp_generate(self._h, n, seed, gamma, None if raw is None else raw.ctypes.data) != 0:
+            raise RuntimeError(last_error())
+        return raw
+
+    def data(self, n: int):
+        X = np.zeros((n, 6), np.float32)
+        Y = np.zeros(n, np.float32)
+        if lib().hydro_mlp_get_data(self._h, X.ctypes.data, Y.ctypes.data, n) != 0:
+            raise RuntimeError(last_error())
+        return X, Y
+
+    def train(self, epochs: int, batch: int = 8192, lr: float = 3e-3, holdout: int = 0):
+        losses = np.zeros(epochs, np.float32)
+        if lib().hydro_mlp_train(self._h, epochs, batch, lr, holdout, losses.ctypes.data) != 0:
+            raise RuntimeError(last_error())
+        return losses
+
+    def gradient(self, X, Y):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        g = np.zeros(MLP_NPARAM, np.float32)
+        loss = ctypes.c_float()
+        if lib().hydro_mlp_gradient(self._h, X, Y, len(Y), g, ctypes.byref(loss)) != 0:
+            raise RuntimeError(last_error())
+        return g, float(loss.value)
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros(len(X), np.float32)
+        if lib().hydro_mlp_predict(self._h, X, len(X), Y) != 0:
+            raise RuntimeError(last_error())
+        return Y
+
+
+def features(states, gamma=1.4):
+    """Device feature map of rows (rhoL, uL, pL, rhoR, uR, pR)."""
+    states = np.ascontiguousarray(states, np.float64)
+    X = np.zeros((len(states), 6), np.float32)
+    if lib().hydro_mlp_features(states, len(states), gamma, X) != 0:
+        raise RuntimeError(last_error())
+    return X
+
+
+def load_weights(path: str = WEIGHTS_PATH) -> np.ndarray:
+    w = np.fromfile(path, dtype="<f4")
+    if w.size != MLP_NPARAM:
+        raise ValueError(f"{path}: {w.size} values, expected {MLP_NPARAM}")
+    return w

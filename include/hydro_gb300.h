@@ -136,6 +136,33 @@ int hydro2d_autotune(hydro2d_t *h, const double *cfg, int ncfg, int steps, float
  * stream).  Nothing is allocated or freed; the call waits for its stream. */
 int hydro1d_run_noalloc(int m, double *d_state, const double *cfg, int ncfg, int order, void *stream,
                         hydro_run_info *info);
+/* ---- learned Newton starting pressure (no reference counterpart) ---------
+ * A 6-64-64-1 ReLU network predicting log(p_star / sqrt(pL pR)) of a Riemann problem
+ * from scale-free features; trained on the GPU by this library's own
+ * forward/backward/Adam kernels on problems labelled by the FP64 exact solver.
+ * Parameters are a flat float[4673]: W1[64][6], b1[64], W2[64][64], b2[64],
+ * w3[64], b3. */
+typedef struct hydro_mlp hydro_mlp_t;
+int hydro_mlp_create(hydro_mlp_t **out, unsigned long long seed);
+void hydro_mlp_destroy(hydro_mlp_t *h);
+int hydro_mlp_get_params(hydro_mlp_t *h, float *params);
+int hydro_mlp_set_params(hydro_mlp_t *h, const float *params);
+/* n problems (density/pressure ratios log-uniform in [1e-4,1e4], velocity jump
+ * uniform in [-5,5]) generated and labelled on the device; raw_host (may be
+ * NULL) receives rhoL,uL,pL,rhoR,uR,pR per problem. */
+int hydro_mlp_generate(hydro_mlp_t *h, long long n, unsigned long long seed, double gamma, double *raw_host);
+int hydro_mlp_get_data(hydro_mlp_t *h, float *X, float *Y, long long n);
+/* Adam with a cosine learning-rate schedule; the last `holdout` problems are
+ * not trained on; loss_per_epoch (may be NULL) gets the mean squared error. */
+int hydro_mlp_train(hydro_mlp_t *h, int epochs, int batch, float lr, long long holdout, float *loss_per_epoch);
+/* Mean squared error and its gradient over n host samples (X[n][6], Y[n]). */
+int hydro_mlp_gradient(hydro_mlp_t *h, const float *X, const float *Y, int n, float *grad, float *loss);
+/* Tensor-core (BF16 mma) inference on host feature rows. */
+int hydro_mlp_predict(hydro_mlp_t *h, const float *X, int n, float *Y);
+/* The device feature map of states rhoL,uL,pL,rhoR,uR,pR (rows of 6). */
+int hydro_mlp_features(const double *states, int n, double gamma, float *X);
+/* Install network parameters into a solver of the HYDRO_FORM_FP32_LEARNED form. */
+int hydro2d_set_mlp(hydro2d_t *h, const float *params);
 /* Number of CUDA kernels launched by this library since load (all solvers). */
 unsigned long long hydro_gb300_kernel_launches(void);
 /* Message of the last failing call in this thread ("" if none). */

@@ -22,6 +22,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libhydro_oracle.so")
+CRPOW_SO = os.path.join(HERE, "_build", "libhydro_oracle_crpow.so")
 REF_SO = os.path.join(HERE, "_ref", "libhydro_ref.so")
 # Where oracle/Makefile finds the reference sources (only needed to build REF_SO).
 REF_TREE = os.environ.get("HYDRO_REFERENCE", "/root/reference")
@@ -72,12 +73,14 @@ def default_config_1d(**kw) -> np.ndarray:
 
 class Oracle:
     def __init__(self, which: str = "port"):
-        path = PORT_SO if which == "port" else REF_SO
+        """which: "port" (the C restatement), "crpow" (the same with a correctly
+        rounded pow) or "reference" (the reference's own sources)."""
+        path = {"port": PORT_SO, "crpow": CRPOW_SO}.get(which, REF_SO)
         if not os.path.exists(path):
             raise FileNotFoundError(f"oracle library missing: {path} (run make -C oracle)")
         self.which = which
         self.lib = ctypes.CDLL(path)
-        p = "orc_" if which == "port" else "ref_"
+        p = "ref_" if which == "reference" else "orc_"
         L = self.lib
         self._run2d = getattr(L, p + "run_2d")
         self._run2d.argtypes = [_int, _int, _dp, _dp, _dp, _dp, _dp, _dp, _int, _int, _int,
@@ -94,7 +97,7 @@ class Oracle:
         self._q1d.argtypes = [_int, _dp, _dbl, _dbl, _dp]
         self._g1d = getattr(L, p + "grp1d")
         self._g1d.argtypes = [_int, _dp, _dbl, _dbl, _dp]
-        if which == "port":
+        if which != "reference":
             self._rexi = L.orc_riemann_exact_iters
             self._rexi.argtypes = [_int, _dp, _dbl, _dbl, _int, _dp]
 

@@ -154,18 +154,18 @@ def main():
 
     if args.large:
         m = n = 1024
-        steps = 500
         rho, u, v, p = cases.four_quadrant(m, n, seed=2024)
-        cfg = orc.default_config_2d(t_all=-1, steps=steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
-        out = R.run_2d(rho, u, v, p, cfg)
-        summ = {"meta": np.array([out["steps"], out["time"], out["wall"]]), "cfg": cfg}
-        for f in ("rho", "u", "v", "p", "E"):
-            summ[f"abs_sum/{f}"] = np.abs(out[f]).sum()
-            summ[f"sum/{f}"] = out[f].sum()
-            summ[f"sub/{f}"] = out[f][::16, ::16].copy()
-            summ[f"row/{f}"] = out[f][m // 2 + 3, :].copy()
-            summ[f"col/{f}"] = out[f][:, n // 2 - 5].copy()
-        np.savez_compressed(os.path.join(HERE, "fq1024_500.npz"), **summ)
+        for steps in (100, 500):
+            cfg = orc.default_config_2d(t_all=-1, steps=steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
+            out = R.run_2d(rho, u, v, p, cfg)
+            summ = {"meta": np.array([out["steps"], out["time"], out["wall"]]), "cfg": cfg}
+            for f in ("rho", "u", "v", "p", "E"):
+                summ[f"abs_sum/{f}"] = np.abs(out[f]).sum()
+                summ[f"sum/{f}"] = out[f].sum()
+                summ[f"sub/{f}"] = out[f][::16, ::16].copy()
+                summ[f"row/{f}"] = out[f][m // 2 + 3, :].copy()
+                summ[f"col/{f}"] = out[f][:, n // 2 - 5].copy()
+            np.savez_compressed(os.path.join(HERE, f"fq1024_{steps}.npz"), **summ)
     print("fixtures written to", HERE)
 
 

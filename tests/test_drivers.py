@@ -1,0 +1,83 @@
+"""End to end through the C99 drivers: data_in text files -> hydrocode_[12]D.out
+(the library's scheme call) -> data_out %.10g text files, with the reference's
+directory conventions (the drivers run from <root>/src/hydrocode_[12]D and read
+../../data_in, write ../../data_out), compared with the oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BUILD = os.path.join(ROOT, "hydrocode-fusion_gb300", "_build")
+
+
+def _write_grid(path, arr2d_rows):
+    with open(path, "w") as f:
+        for row in arr2d_rows:
+            f.write("\t".join(f"{x:.17g}" for x in row) + "\n")
+
+
+def _read_dat(path, nrows=None):
+    rows = []
+    for line in open(path):
+        line = line.strip()
+        if line:
+            rows.append([float(x) for x in line.split()])
+    return np.array(rows)
+
+
+@pytest.mark.gpu
+def test_2d_driver_end_to_end(gpu_lib, port, tmp_path):
+    hg = gpu_lib
+    from hydro_gb300 import cases
+
+    exe = os.path.join(BUILD, "hydrocode_2D.out")
+    assert os.path.exists(exe)
+    m, n = 30, 20  # x cells (columns), y cells (lines)
+    rho, u, v, p = cases.four_quadrant(m, n, seed=12)
+    case = tmp_path / "data_in" / "two-dim" / "FQ"
+    case.mkdir(parents=True)
+    for name, a in (("RHO", rho), ("U", u), ("V", v), ("P", p)):
+        _write_grid(case / f"{name}.txt", a.T)  # file line i = y index i
+    (case / "config.txt").write_text("1 -1\n5 25\n4 1e-9\n6 1.4\n7 0.45\n10 %r\n11 %r\n17 -4\n18 -4\n" % (1 / m, 1 / n))
+    run_dir = tmp_path / "src" / "hydrocode_2D"
+    run_dir.mkdir(parents=True)
+    r = subprocess.run([exe, "FQ", "fq_out", "2", "EUL"], cwd=run_dir, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = tmp_path / "data_out" / "two-dim" / "EUL_2_order" / "fq_out"
+    cfg = hg.config_2d(t_all=-1, steps=25, hx=1 / m, hy=1 / n, bx=-4, by=-4)
+    want = port.run_2d(rho, u, v, p, cfg)
+    for name, key in (("RHO", "rho"), ("U", "u"), ("V", "v"), ("P", "p"), ("E", "E")):
+        got = _read_dat(out / f"{name}.dat")
+        assert got.shape == (2 * n, m)  # initial and final state, one line per y row
+        np.testing.assert_allclose(got[n:].T, want[key], rtol=2e-10, atol=1e-12)
+        np.testing.assert_allclose(got[:n].T, {"rho": rho, "u": u, "v": v, "p": p}.get(key, got[:n].T), rtol=2e-10)
+    assert (out / "log.dat").exists() and (out / "time_plot.dat").exists()
+    assert any(f.name.startswith("FLU_VAR_") for f in out.iterdir())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2])
+def test_1d_driver_sod(gpu_lib, tmp_path, order):
+    exe = os.path.join(BUILD, "hydrocode_1D.out")
+    from hydro_gb300 import cases
+
+    rho, u, p = cases.sod(400)
+    case = tmp_path / "data_in" / "one-dim" / "SOD"
+    case.mkdir(parents=True)
+    for name, a in (("RHO", rho), ("U", u), ("P", p)):
+        (case / f"{name}.txt").write_text("\n".join(f"{x:.17g}" for x in a) + "\n")
+    (case / "config.txt").write_text("1 0.2\n4 1e-9\n5 100000\n6 1.4\n7 0.45\n10 0.0025\n17 -4\n")
+    run_dir = tmp_path / "src" / "hydrocode_1D"
+    run_dir.mkdir(parents=True)
+    r = subprocess.run([exe, "SOD", "sod_out", str(order), "EUL"], cwd=run_dir, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = tmp_path / "data_out" / "one-dim" / f"EUL_{order}_order" / "sod_out"
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "runs_1d.npz"))
+    for name, key in (("RHO", "rho"), ("U", "u"), ("P", "p")):
+        got = _read_dat(out / f"{name}.dat")
+        np.testing.assert_allclose(got[-1], gold[f"sod{order}/{key}"], rtol=2e-10, atol=1e-12)
+    tp = _read_dat(out / "time_plot.dat").ravel()
+    assert abs(tp[-1] - 0.2) < 1e-12
