@@ -3,6 +3,7 @@
 // planning and error reporting.  Host code only; the kernels live in the
 // per-precision translation units.
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -139,6 +140,30 @@ static int form_from_config(const double* cfg)
     return (int)f;
 }
 
+// The trained network shipped with the library: $HYDRO_MLP_WEIGHTS, else
+// weights/riemann_guess_6_64_64_1.f32 next to the library's build folder.
+static bool default_mlp(std::vector<float>& w, std::string& path)
+{
+    if (const char* e = getenv("HYDRO_MLP_WEIGHTS")) {
+        path = e;
+    } else {
+        Dl_info di;
+        if (!dladdr((void*)&default_mlp, &di) || !di.dli_fname)
+            return false;
+        std::string so = di.dli_fname;
+        size_t cut = so.rfind('/');
+        std::string dir = cut == std::string::npos ? std::string(".") : so.substr(0, cut);
+        path = dir + "/../weights/riemann_guess_6_64_64_1.f32";
+    }
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f)
+        return false;
+    w.assign(HYDRO_MLP_NPARAM, 0.f);
+    size_t got = fread(w.data(), sizeof(float), w.size() + 1, f);
+    fclose(f);
+    return got == w.size();
+}
+
 static Solver2DBase* make_solver(int m, int n, int form)
 {
     switch (form) {
@@ -146,8 +171,17 @@ static Solver2DBase* make_solver(int m, int n, int form)
         return make_solver2d_f64(m, n);
     case HYDRO_FORM_FP32:
         return make_solver2d_f32(m, n, 0);
-    case HYDRO_FORM_FP32_LEARNED:
-        return make_solver2d_f32(m, n, 1);
+    case HYDRO_FORM_FP32_LEARNED: {
+        Solver2DBase* s = make_solver2d_f32(m, n, 1);
+        if (!s)
+            return nullptr;
+        // install the shipped network when it is there (hydro2d_set_mlp replaces it)
+        std::vector<float> w;
+        std::string path;
+        if (default_mlp(w, path))
+            s->set_mlp(w.data());
+        return s;
+    }
     default:
         set_error("unknown form");
         return nullptr;

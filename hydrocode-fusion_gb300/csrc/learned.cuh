@@ -24,10 +24,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/hydro_gb300.h"
+
 namespace hydro {
 
 constexpr int MLP_IN = 6, MLP_H = 64;
 constexpr int MLP_NPARAM = MLP_H * MLP_IN + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1;  // 4673
+static_assert(MLP_NPARAM == HYDRO_MLP_NPARAM, "parameter count of the C ABI");
 // offsets in the flat FP32 parameter vector
 constexpr int MLP_W1 = 0, MLP_B1 = MLP_W1 + MLP_H * MLP_IN, MLP_W2 = MLP_B1 + MLP_H,
               MLP_B2 = MLP_W2 + MLP_H * MLP_H, MLP_W3 = MLP_B2 + MLP_H, MLP_B3 = MLP_W3 + MLP_H;

@@ -283,22 +283,20 @@ struct UnsplitSmem {
     static constexpr size_t bytes_learned = (bytes + 15) / 16 * 16 + sizeof(MlpShared);
 };
 
-template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
-__global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
+// One TJ x TI tile (cells i in [I0, I0+TI), j in [J0, J0+TJ)) of the unsplit
+// step, computed by a block of NT threads; used by the one-problem kernel
+// below and by the batched persistent kernel.  Ends with a block barrier, so
+// the shared memory can be reused for the next tile at once.
+template <typename R, int TJ, int TI, int NT, bool LEARNED>
+__device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0, const int J0, unsigned char* smem_raw,
+                                             const MlpShared& Mlp)
 {
     using SM = UnsplitSmem<R, TJ, TI>;
-    if (halt_prologue(a.ctl, a.seq))
-        return;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     R* W = reinterpret_cast<R*>(smem_raw);
     R* S = W + SM::nW;
     R* FX = S + SM::nS;
     R* FY = FX + SM::nFX;
-    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + (SM::bytes + 15) / 16 * 16);
-    if (LEARNED)
-        mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
     const int tid = threadIdx.x;
-    const int I0 = blockIdx.x * TI, J0 = blockIdx.y * TJ;
     const int m = a.m, n = a.n, slot = a.seq % 3;
     constexpr int WJ = SM::WJ, WI = SM::WI, SJ = SM::SJ, SI = SM::SI;
 #define Wx(k, lj, li) W[((k) * WJ + (lj)) * WI + (li)]
@@ -510,10 +508,24 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
     }
     if (bad)
         atomicOr(&a.ctl->upd_bad[slot], 1u);
+    __syncthreads();
 #undef Wx
 #undef Sx
 #undef FXx
 #undef FYx
+}
+
+template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
+__global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
+{
+    using SM = UnsplitSmem<R, TJ, TI>;
+    if (halt_prologue(a.ctl, a.seq))
+        return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + (SM::bytes + 15) / 16 * 16);
+    if (LEARNED)
+        mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
+    unsplit_tile<R, TJ, TI, NT, LEARNED>(a, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
 }
 
 // ---------------------------------------------------------------------------

@@ -47,6 +47,27 @@ class RunInfo(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("gpu_ms", ctypes.c_double),
+        ("shape", ctypes.c_int),
+        ("schedule", ctypes.c_int),
+        ("graphed", ctypes.c_int),
+        ("steps", ctypes.c_int),
+        ("tiles", ctypes.c_int),
+        ("halted_problems", ctypes.c_int),
+        ("newton_faces", ctypes.c_ulonglong),
+        ("newton_iters", ctypes.c_ulonglong),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+SCHEDULES = ("persistent-static", "persistent-static-largest-first", "persistent-dynamic",
+             "persistent-dynamic-largest-first", "graph-per-step")
+
+
 def build(jobs: int = 4) -> str:
     """Compile the library in-tree (nvcc, sm_103a) and return its path."""
     subprocess.run(["make", "-s", "-j", str(jobs), "-C", PKG_DIR], check=True)
@@ -91,6 +112,18 @@ def lib() -> ctypes.CDLL:
     L.hydro_mlp_gradient.argtypes = [vp, _fp, _fp, ctypes.c_int, _fp, ctypes.POINTER(ctypes.c_float)]
     L.hydro_mlp_predict.argtypes = [vp, _fp, ctypes.c_int, _fp]
     L.hydro_mlp_features.argtypes = [_dp, ctypes.c_int, ctypes.c_double, _fp]
+    L.hydro_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.hydro_batch_destroy.argtypes = [vp]
+    L.hydro_batch_destroy.restype = None
+    L.hydro_batch_upload.argtypes = [vp, ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_void_p, ctypes.c_double]
+    L.hydro_batch_download.argtypes = [vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
+    L.hydro_batch_run.argtypes = [vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(BatchInfo)]
+    L.hydro_batch_shape.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.hydro_batch_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.hydro_batch_set_wait_limit.argtypes = [vp, ctypes.c_double]
+    L.hydro_batch_autotune.argtypes = [vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    L.hydro_batch_problem_info.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.hydro_gb300_last_error.restype = ctypes.c_char_p
     L.hydro_gb300_kernel_launches.restype = ctypes.c_ulonglong
     _lib = L
@@ -301,3 +334,81 @@ def load_weights(path: str = WEIGHTS_PATH) -> np.ndarray:
     if w.size != MLP_NPARAM:
         raise ValueError(f"{path}: {w.size} values, expected {MLP_NPARAM}")
     return w
+
+
+class Batch:
+    """Many independent 2D problems of uneven size, advanced together in the
+    FP32 form (hydro_batch_* in the C ABI).  sizes: list of (m, n)."""
+
+    def __init__(self, sizes):
+        self.sizes = [(int(m), int(n)) for m, n in sizes]
+        ms = (ctypes.c_int * len(self.sizes))(*[m for m, _ in self.sizes])
+        ns = (ctypes.c_int * len(self.sizes))(*[n for _, n in self.sizes])
+        h = ctypes.c_void_p()
+        if lib().hydro_batch_create(ctypes.byref(h), len(self.sizes), ms, ns) != 0:
+            raise RuntimeError("hydro_batch_create failed: " + last_error())
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().hydro_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, p, rho, u, v, pr, gamma=1.4):
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (rho, u, v, pr)]
+        for a in arrs:
+            assert a.shape == self.sizes[p]
+        if lib().hydro_batch_upload(self._h, p, *arrs, None, gamma) != 0:
+            raise RuntimeError("batch upload failed: " + last_error())
+
+    def download(self, p):
+        out = [np.empty(self.sizes[p]) for _ in range(5)]
+        if lib().hydro_batch_download(self._h, p, *out) != 0:
+            raise RuntimeError("batch download failed: " + last_error())
+        return dict(zip(("rho", "u", "v", "p", "E"), out))
+
+    def set_schedule(self, shape, schedule):
+        if lib().hydro_batch_set_schedule(self._h, int(shape), int(schedule)) != 0:
+            raise RuntimeError(last_error())
+
+    def set_wait_limit(self, seconds):
+        if lib().hydro_batch_set_wait_limit(self._h, float(seconds)) != 0:
+            raise RuntimeError(last_error())
+
+    @staticmethod
+    def shapes():
+        out = []
+        for k in range(lib().hydro_batch_num_shapes()):
+            s = (ctypes.c_int * 4)()
+            lib().hydro_batch_shape(k, s)
+            out.append({"tile_x": s[0], "tile_y": s[1], "threads": s[2], "min_ctas_per_sm": s[3]})
+        return out
+
+    def autotune(self, cfg, steps=3):
+        cfg = np.ascontiguousarray(cfg, np.float64)
+        nsh, nsc = lib().hydro_batch_num_shapes(), lib().hydro_batch_num_schedules()
+        times = (ctypes.c_float * (nsh * nsc))()
+        best = lib().hydro_batch_autotune(self._h, cfg, len(cfg), int(steps), times)
+        if best < 0:
+            raise RuntimeError("batch autotune failed: " + last_error())
+        return int(best), np.array(list(times), np.float64).reshape(nsh, nsc)
+
+    def run(self, cfg, steps, stats=False) -> BatchInfo:
+        cfg = np.ascontiguousarray(cfg, np.float64)
+        info = BatchInfo()
+        rc = lib().hydro_batch_run(self._h, cfg, len(cfg), int(steps), int(bool(stats)), ctypes.byref(info))
+        if rc != 0:
+            raise RuntimeError(f"batch run failed ({rc}): " + last_error())
+        return info
+
+    def problem_info(self, p):
+        k, s, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        if lib().hydro_batch_problem_info(self._h, p, ctypes.byref(k), ctypes.byref(s), ctypes.byref(t)) != 0:
+            raise RuntimeError(last_error())
+        return {"halted": k.value, "halted_step": s.value, "tau": t.value}

@@ -49,3 +49,15 @@ def sod(m: int = 400):
     u = np.zeros(m)
     p = np.where(x < 0.5, 1.0, 0.1)
     return rho, u, p
+
+
+def batch_sizes(count: int = 512, seed: int = 4, lo: int = 64, hi: int = 512, step: int = 32):
+    """Square grid sizes N x N with N drawn uniformly from {lo, lo+step, ..., hi}."""
+    rng = np.random.default_rng(seed)
+    choices = np.arange(lo, hi + 1, step)
+    return [(int(N), int(N)) for N in rng.choice(choices, count)]
+
+
+def batch_problems(sizes, seed: int = 4):
+    """Seeded four-quadrant data for every grid of a batch (problem k uses seed*100003 + k)."""
+    return [four_quadrant(m, n, seed * 100003 + k) for k, (m, n) in enumerate(sizes)]

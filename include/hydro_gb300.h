@@ -142,6 +142,11 @@ int hydro1d_run_noalloc(int m, double *d_state, const double *cfg, int ncfg, int
  * forward/backward/Adam kernels on problems labelled by the FP64 exact solver.
  * Parameters are a flat float[4673]: W1[64][6], b1[64], W2[64][64], b2[64],
  * w3[64], b3. */
+#define HYDRO_MLP_NPARAM 4673
+/* A solver of the learned form installs the trained network shipped with the
+ * library when it is created: the file named by $HYDRO_MLP_WEIGHTS, else
+ * weights/riemann_guess_6_64_64_1.f32 beside the library's build folder
+ * (so GRP_solver_2D_EUL_source with config[300] = 2 needs no extra call). */
 typedef struct hydro_mlp hydro_mlp_t;
 int hydro_mlp_create(hydro_mlp_t **out, unsigned long long seed);
 void hydro_mlp_destroy(hydro_mlp_t *h);
@@ -163,6 +168,67 @@ int hydro_mlp_predict(hydro_mlp_t *h, const float *X, int n, float *Y);
 int hydro_mlp_features(const double *states, int n, double gamma, float *X);
 /* Install network parameters into a solver of the HYDRO_FORM_FP32_LEARNED form. */
 int hydro2d_set_mlp(hydro2d_t *h, const float *params);
+/* ---- batched problems (no reference counterpart) --------------------------
+ * Many independent 2D unsplit GRP problems of uneven grid size m x n on the
+ * unit square (h_x = 1/m, h_y = 1/n) advanced together for a fixed number of
+ * steps in the FP32 form.  Each problem has its own CFL time step from its own
+ * initial data (as grp_solver_2D_EUL_source.c:180-200 does for one grid) and
+ * its own halting; its result equals a one-problem FP32 run of that grid.
+ * config[] supplies gamma, eps, CFL, alpha and the boundary codes (17, 18) for
+ * all problems; t_all is ignored.
+ * Schedules: 0/1 persistent cooperative kernel, static tiles (problem-major /
+ * largest problem first), 2/3 the same with a dynamic tile counter, 4 a CUDA
+ * graph of one launch per step.  The persistent kernel separates the steps
+ * with a grid barrier whose wait is limited (default 5 s,
+ * hydro_batch_set_wait_limit); a wait that runs out makes the run return -2. */
+typedef struct hydro_batch hydro_batch_t;
+typedef struct {
+    double gpu_ms;            /* device time of the time loop */
+    int shape, schedule;      /* tile shape index and schedule used */
+    int graphed;              /* 1 if the time loop ran as one captured CUDA graph */
+    int steps, tiles;         /* steps run; tiles per step over all problems */
+    int halted_problems;      /* problems that stopped or aborted early */
+    unsigned long long newton_faces, newton_iters; /* with stats = 1 */
+} hydro_batch_info;
+int hydro_batch_create(hydro_batch_t **out, int nprob, const int *m, const int *n);
+void hydro_batch_destroy(hydro_batch_t *b);
+/* x-major planes of problem p (E may be NULL: computed as the 2D driver does). */
+int hydro_batch_upload(hydro_batch_t *b, int p, const double *rho, const double *u, const double *v, const double *pr,
+                       const double *E, double gamma);
+int hydro_batch_download(hydro_batch_t *b, int p, double *rho, double *u, double *v, double *pr, double *E);
+int hydro_batch_run(hydro_batch_t *b, const double *cfg, int ncfg, int steps, int stats, hydro_batch_info *info);
+int hydro_batch_num_shapes(void);
+int hydro_batch_num_schedules(void);
+/* out4 = {tile cells along y, along x, threads, min CTAs per SM} */
+int hydro_batch_shape(int shape, int *out4);
+int hydro_batch_set_schedule(hydro_batch_t *b, int shape, int schedule);
+int hydro_batch_set_wait_limit(hydro_batch_t *b, double seconds);
+/* Times every (shape, schedule) pair on `steps` steps of the uploaded states
+ * (restored afterwards), keeps the fastest and returns shape * schedules +
+ * schedule; times_ms (may be NULL) receives shapes x schedules values. */
+int hydro_batch_autotune(hydro_batch_t *b, const double *cfg, int ncfg, int steps, float *times_ms);
+/* Outcome of problem p in the last run: halted (0 no, 1 abort, 2 stop), the
+ * step it halted on, and its time step. */
+int hydro_batch_problem_info(hydro_batch_t *b, int p, int *halted, int *halted_step, double *tau);
+
+/* One-call form: create, upload, (autotune), run, download, destroy. */
+typedef struct {
+    int m, n;                 /* grid size */
+    double *rho, *u, *v, *p;  /* x-major [m][n]: initial state in, final state out */
+    double *E;                /* may be NULL on input (computed) -- then not written */
+    int halted, halted_step;  /* out */
+    double tau;               /* out: the problem's time step */
+} hydro_problem;
+typedef struct {
+    const double *cfg;        /* config[] */
+    int ncfg;
+    int autotune_steps;       /* > 0: autotune on that many steps first */
+    int shape, schedule;      /* used when not autotuning */
+    int stats;
+    hydro_batch_info info;    /* out */
+} hydro_batch_opts;
+int hydro_gb300_batch_run(hydro_problem *probs, int nprob, int steps, hydro_batch_opts *o);
+
 /* Number of CUDA kernels launched by this library since load (all solvers). */
 unsigned long long hydro_gb300_kernel_launches(void);
 /* Message of the last failing call in this thread ("" if none). */

