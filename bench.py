@@ -1,26 +1,35 @@
 """Benchmark: 2D GRP cell-updates/s at 4096^2 on one GB300.
 
-A "step" is one time step of the 2D unsplit GRP scheme over the whole grid
-(seeded four-quadrant Riemann data, transmissive boundaries, CFL 0.45).
-value      : FP32 form (learned starting pressure when available), device
-             resident state, CUDA-event time of the K timed steps.
-e2e        : the same metric through the reference's C entry point
-             GRP_solver_2D_EUL_source with host arrays (upload, K steps,
-             download inside the timed region).
-fp64       : the plain FP64 parity form on the same grid (fewer steps).
-roofline   : HBM roofline of the step kernel from its algorithmic bytes
-             (96 B per cell-update in FP32: rho,u,v,p + 8 slopes read and written).
-cpu_baseline: the oracle port of the reference's CPU path (OpenMP, all host
-             threads) on a bounded sample of the same grid.
+Workload: the 2D unsplit GRP scheme (the reference's GRP_solver_2D_EUL_source)
+on a 4096 x 4096 grid over [0,1]^2, seeded four-quadrant Riemann data
+(rho, p ~ U[0.1,2], u, v ~ U[-1,1], seed 2024), transmissive boundaries,
+gamma 1.4, CFL 0.45.  A "step" is one time step over the whole grid.
 
---impl reference times that CPU path alone on the same workload.
+value       FP32 form with the learned Newton starting pressure (the headline
+            form), state resident in HBM, CUDA-event time of K steps on the
+            solver's stream (inputs of 13 planes x 4 B x 16.8 M cells, far
+            larger than L2, so no flush is needed between steps).
+e2e         the same form through the reference's scheme call
+            GRP_solver_2D_EUL_source (config[300] = 2) from host arrays:
+            upload, K steps, download and the call's own set-up inside the
+            timed region (wall clock around the call).
+forms       plain FP32 and the FP64 parity form on the same grid and steps,
+            relative L1 of every FP32 result against the FP64 result, FP64
+            conservation integrals, Newton statistics.
+roofline    HBM roofline of the step kernel: 104 algorithmic bytes per
+            FP32 cell-update (13 planes read, 13 written, 4 B each).
+batch       512 independent four-quadrant problems, N x N with N uniform in
+            {64, 96, ..., 512}, 300 steps, one persistent kernel under a CUDA
+            graph with the autotuned tile shape and schedule.
+cpu_baseline the oracle's C restatement of the reference's CPU path (OpenMP,
+            all host cores) on a bounded number of steps of the same grid.
+
+--impl reference times that CPU path alone on the same workload and metric.
 """
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
-import math
 import os
 import subprocess
 import sys
@@ -33,6 +42,11 @@ sys.path.insert(0, PKG)
 
 import numpy as np  # noqa: E402
 
+METRIC = "2D GRP cell-updates/s at 4096^2"
+UNIT = "cell-updates/s"
+BYTES_PER_CELL_F32 = 104.0   # 13 planes read + 13 written, 4 B
+BYTES_PER_CELL_F64 = 208.0
+
 
 def peaks():
     try:
@@ -41,6 +55,15 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def traffic_per_cell(kernel_key):
+    """DRAM bytes per cell-update of a kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return float(json.load(f)[kernel_key]["dram_bytes_per_cell"])
+    except Exception:
+        return None
 
 
 class ClockSampler:
@@ -54,12 +77,13 @@ class ClockSampler:
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
-                                          f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", dev, f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            time.sleep(0.3)
         except Exception:
             self.proc = None
         return self
@@ -81,15 +105,24 @@ class ClockSampler:
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [v for v in (num(s[0]) for s in self.samples) if v is not None]
+        mx = [v for v in (num(s[1]) for s in self.samples) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_baseline(m, n, steps, threads):
+def cpu_rate(m, n, steps, threads):
+    """The oracle's C restatement of the reference's 2D unsplit GRP loop on the
+    host cores; returns (cell-updates/s, seconds of the scheme call)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     from hydro_gb300 import cases
@@ -98,12 +131,155 @@ def cpu_baseline(m, n, steps, threads):
         orc.build()
     port = orc.Oracle("port")
     rho, u, v, p = cases.four_quadrant(m, n, seed=2024)
+    cfg1 = orc.default_config_2d(t_all=-1, steps=1, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
+    port.run_2d(rho, u, v, p, cfg1, threads=threads)  # pages the code and data in
     cfg = orc.default_config_2d(t_all=-1, steps=steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
-    t0 = time.perf_counter()
     out = port.run_2d(rho, u, v, p, cfg, threads=threads)
+    return m * n * steps / out["wall"], out["wall"]
+
+
+def rel_l1(a, b):
+    d = np.abs(b).sum()
+    return float(np.abs(a - b).sum() / d) if d > 0 else float(np.abs(a - b).sum())
+
+
+def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dist=None):
+    """Tune, warm up, then time K steps of one form from the initial state.
+    Returns a dict with the rate, the final state and statistics."""
+    rho, u, v, p = state
+    cfgK = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
+    cfgW = hg.config_2d(t_all=-1, steps=W, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
+    s = hg.Solver2D(m, n, form)
+    res = {}
+    try:
+        if form == hg.FORM_FP32_LEARNED:
+            s.set_mlp(hg.load_weights())
+        s.upload(rho, u, v, p)
+        if tune:
+            best, times = s.autotune(cfgW, steps=3)
+            res["autotune"] = {"best": best, "ms_per_3_steps": [round(t, 3) for t in times]}
+        res["kernel_variant"] = s.variant()[1]
+        s.run(cfgW)
+        s.upload(rho, u, v, p)
+        res["conservation_initial"] = s.conservation()
+        import torch
+
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        l0 = hg.kernel_launches()
+        sampler = ClockSampler() if clocks else None
+        if sampler:
+            sampler.__enter__()
+        info = s.run(cfgK)
+        if sampler:
+            sampler.__exit__(None, None, None)
+        torch.cuda.synchronize()
+        res["launches"] = hg.kernel_launches() - l0
+        ms = info.gpu_ms
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        res["gpu_ms"] = ms
+        res["ms_per_step"] = ms / K
+        res["value"] = m * n * K / (ms * 1e-3)
+        res["steps_done"] = info.steps_done
+        res["halted"] = info.halted
+        res["clocks"] = sampler.summary() if sampler else None
+        res["conservation_final"] = s.conservation()
+        res["state"] = s.download()
+        if stats_steps > 0:
+            s.upload(rho, u, v, p)
+            i2 = s.run(hg.config_2d(t_all=-1, steps=stats_steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), stats=True)
+            faces = 2.0 * m * n * stats_steps
+            res["newton"] = {"steps": stats_steps, "exact_solves_per_face": i2.newton_faces / faces,
+                             "iters_per_exact_solve": (i2.newton_iters / i2.newton_faces) if i2.newton_faces else 0.0,
+                             "fp64_fallbacks_per_exact_solve": (i2.newton_fallbacks / i2.newton_faces)
+                             if i2.newton_faces else 0.0}
+    finally:
+        s.close()
+    return res
+
+
+def e2e_run(hg, state, m, n, K):
+    """The learned form through GRP_solver_2D_EUL_source with host arrays."""
+    from hydro_gb300.dropin import Call2D
+
+    rho, u, v, p = state
+    cfg = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4, form=hg.FORM_FP32_LEARNED)
+    c = Call2D(hg.lib(), rho, u, v, p, 1.4, cfg, N_MAX=2)
+    l0 = hg.kernel_launches()
+    t0 = time.perf_counter()
+    nplot, k_out = c.call()
     wall = time.perf_counter() - t0
-    loop = out["wall"]  # time of the scheme call itself (allocation + loop)
-    return m * n * steps / loop, loop, wall
+    launches = hg.kernel_launches() - l0
+    plane_bytes = 8 * m * n
+    return {"value": m * n * K / wall, "unit": UNIT, "h2d_bytes_per_step": 5 * plane_bytes / K,
+            "d2h_bytes_per_step": 5 * plane_bytes / K, "wall_s": wall, "k_out": int(k_out), "launches": int(launches),
+            "call": "GRP_solver_2D_EUL_source, config[300]=2, host x-major row arrays (CV[0] in, CV[1] out)"}
+
+
+def batch_run(hg, count, steps, tune_steps, l1_sample):
+    from hydro_gb300 import cases
+
+    sizes = cases.batch_sizes(count, seed=4)
+    probs = cases.batch_problems(sizes, seed=4)
+    cfg = hg.config_2d(t_all=-1, steps=steps, bx=-4, by=-4)
+    b = hg.Batch(sizes)
+    try:
+        for k, pr in enumerate(probs):
+            b.upload(k, *pr)
+        best, times = b.autotune(cfg, steps=tune_steps)
+        l0 = hg.kernel_launches()
+        info = b.run(cfg, steps)
+        launches = hg.kernel_launches() - l0
+        cells = sum(mm * nn for mm, nn in sizes)
+        rate = cells * steps / (info.gpu_ms * 1e-3)
+        halted = [k for k in range(count) if b.problem_info(k)["halted"]]
+        sample = sorted(set(list(range(0, count, max(1, count // l1_sample)))[:l1_sample] + halted[:4]))
+        l1 = []
+        for k in sample:
+            mm, nn = sizes[k]
+            got = b.download(k)
+            pi = b.problem_info(k)
+            c64 = hg.config_2d(t_all=-1, steps=steps, hx=1.0 / mm, hy=1.0 / nn, bx=-4, by=-4)
+            want, i64 = hg.run_2d(*probs[k], c64)
+            rec = {"problem": k, "N": mm, "halted_fp32": pi["halted"], "halted_step_fp32": pi["halted_step"],
+                   "halted_fp64": i64.halted, "steps_fp64": i64.steps_done}
+            if not pi["halted"] and not i64.halted:
+                rec.update({f: rel_l1(got[f], want[f]) for f in ("rho", "u", "v", "p")})
+            l1.append(rec)
+    finally:
+        b.close()
+    shapes = hg.Batch.shapes()
+    peak, _ = peaks()
+    return {"problems": count, "sizes": "N x N, N uniform in {64, 96, ..., 512} (seed 4)", "cells": cells,
+            "steps": steps, "value": rate, "unit": UNIT, "gpu_ms": info.gpu_ms,
+            "hbm_frac": BYTES_PER_CELL_F32 * rate / 1e9 / peak,
+            "shape": shapes[info.shape], "schedule": hg.SCHEDULES[info.schedule], "graphed": bool(info.graphed),
+            "autotune_ms_per_%d_steps" % tune_steps: np.round(times, 3).tolist(), "gpu_launches": int(launches),
+            "halted_problems": info.halted_problems, "per_problem_l1_vs_fp64": l1}
+
+
+def reference_arm(args, m, n, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    S = max(1, min(args.steps, args.cpu_steps))
+    rate, loop = cpu_rate(m, n, S, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": loop * 1e3 / S, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_name(m, n), "sample_steps": S},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{m}x{n}, {S} of {args.steps} steps (the reference's loop restated in C, OpenMP)"},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_name(m, n):
+    return f"2D unsplit GRP, {m}x{n} four-quadrant Riemann data (seed 2024), transmissive, gamma 1.4, CFL 0.45"
 
 
 def main():
@@ -113,30 +289,21 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=4096)
-    ap.add_argument("--fp64-steps", type=int, default=20)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=-1, help="FP64 form steps (default: --steps; 0 skips)")
+    ap.add_argument("--stats-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-tune", action="store_true", help="skip the kernel-variant autotuner")
+    ap.add_argument("--no-tune", action="store_true", help="skip the kernel-variant autotuners")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=300)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     m = n = args.size
-    workload = f"2D GRP unsplit, {m}x{n} four-quadrant (seeded), transmissive, CFL 0.45"
-    metric = "2D GRP cell-updates/s at 4096^2"
-    threads = os.cpu_count() or 1
-
     if args.impl == "reference":
-        if rank != 0:
-            return
-        rate, loop, wall = cpu_baseline(m, n, max(1, args.cpu_steps), threads)
-        line = {"impl": "reference", "metric": metric, "value": rate, "unit": "cell-updates/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": loop * 1e3 / max(1, args.cpu_steps),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": workload, "sample_steps": max(1, args.cpu_steps)},
-                "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-                                 "sample": f"{m}x{n}, {max(1, args.cpu_steps)} steps"},
-                "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        reference_arm(args, m, n, rank)
         return
 
     import torch
@@ -145,77 +312,75 @@ def main():
     from hydro_gb300 import cases
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    rho, u, v, p = cases.four_quadrant(m, n, seed=2024)
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+        dist = tdist
+    state = cases.four_quadrant(m, n, seed=2024)
     K, W = args.steps, max(3, args.warmup)
-    form = hg.FORM_FP32
-    cfg_w = hg.config_2d(t_all=-1, steps=W, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
-    cfg_k = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
+    tune = not args.no_tune
+    k64 = K if args.fp64_steps < 0 else args.fp64_steps
 
-    s = hg.Solver2D(m, n, form)
-    s.upload(rho, u, v, p)
-    tune = None
-    if not args.no_tune:
-        best, times = s.autotune(cfg_w, steps=3)
-        tune = {"best": best, "ms_per_3_steps": times}
-    variant = s.variant()
-    s.run(cfg_w)                      # warm-up steps
-    s.upload(rho, u, v, p)
-    torch.cuda.synchronize()
-    l0 = hg.kernel_launches()
-    with ClockSampler() as cs:
-        info = s.run(cfg_k, stats=False)
-    launches = hg.kernel_launches() - l0
-    torch.cuda.synchronize()
-    ms_step = info.gpu_ms / K
-    value = m * n * K / (info.gpu_ms * 1e-3)
-    s.close()
+    head = timed_form(hg, hg.FORM_FP32_LEARNED, state, m, n, K, W, tune, args.stats_steps, clocks=True, dist=dist)
+    if dist is not None:
+        dist.barrier()
+    value = world * head["value"]  # replicas: every rank advances its own grid
+    if rank != 0:
+        return
+    plain = timed_form(hg, hg.FORM_FP32, state, m, n, K, W, tune, args.stats_steps)
+    fp64 = timed_form(hg, hg.FORM_FP64, state, m, n, k64, 3, tune, args.stats_steps) if k64 > 0 else None
 
-    # FP64 parity form, same grid
-    fp64 = None
-    if args.fp64_steps > 0:
-        fp64 = fp64_run(hg, m, n, rho, u, v, p, args)
-    line_fp64 = fp64
+    def accuracy(res):
+        if fp64 is None or k64 != K:
+            return None
+        return {f: rel_l1(res["state"][f], fp64["state"][f]) for f in ("rho", "u", "v", "p")}
+
+    def summary(res, dtype):
+        return {k: v for k, v in res.items() if k not in ("state",)} | {"dtype": dtype}
 
     peak, peak_kind = peaks()
-    alg_bytes = 96.0 * m * n  # per launch: 12 FP32 fields read + written
-    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    ms = head["ms_per_step"]
+    achieved = BYTES_PER_CELL_F32 * m * n / (ms * 1e-3) / 1e9
+    tpc = traffic_per_cell("k_step_unsplit<float,learned>")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "peak_source": peak_kind}
+            "traffic": tpc * m * n if tpc else None, "peak_source": peak_kind,
+            "kernel": "k_step_unsplit<float, learned> (one launch per step)",
+            "algorithmic_bytes_per_launch": BYTES_PER_CELL_F32 * m * n}
+
+    forms = {
+        "fp32_learned": summary(head, "f32") | {"l1_vs_fp64": accuracy(head)},
+        "fp32": summary(plain, "f32") | {"l1_vs_fp64": accuracy(plain)},
+        "fp64": (summary(fp64, "f64") | {
+            "hbm_frac": BYTES_PER_CELL_F64 * fp64["value"] / 1e9 / peak}) if fp64 else None,
+        "speedup_learned_over_fp64": head["value"] / fp64["value"] if fp64 else None,
+    }
+    if fp64:
+        for key in ("fp32_learned", "fp32"):
+            forms[key]["mass_drift_vs_fp64"] = (
+                forms[key]["conservation_final"]["mass"] - fp64["conservation_final"]["mass"]) / fp64[
+                "conservation_final"]["mass"]
+
+    e2e = None if args.no_e2e else e2e_run(hg, state, m, n, K)
+    batch = None if args.no_batch else batch_run(hg, args.batch_count, args.batch_steps, 5, 8)
 
     cpu = None
     if not args.no_cpu:
-        rate, loop, wall = cpu_baseline(m, n, max(1, args.cpu_steps), threads)
-        cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-               "sample": f"{m}x{n}, {max(1, args.cpu_steps)} steps of the FP64 reference arithmetic (OpenMP)"}
+        threads = os.cpu_count() or 1
+        rate, loop = cpu_rate(m, n, max(1, args.cpu_steps), threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{m}x{n}, {args.cpu_steps} steps (the reference's loop restated in C, OpenMP)"}
 
-    line = {"metric": metric, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload, "form": "fp32", "grid": [m, n], "l2": "inputs larger than L2 (13 planes x 4 B x 16.8M cells)",
-                       "kernel_variant": variant, "autotune": tune},
-            "roofline": roof, "cpu_baseline": cpu, "gpu_launches": int(launches),
-            "fp64": line_fp64, "clocks": cs.summary()}
-    if rank == 0:
-        print(json.dumps(line))
-
-
-def fp64_run(hg, m, n, rho, u, v, p, args):
-    s64 = hg.Solver2D(m, n, hg.FORM_FP64)
-    s64.upload(rho, u, v, p)
-    tune64 = None
-    if not args.no_tune and args.fp64_steps > 0:
-        best64, times64 = s64.autotune(hg.config_2d(t_all=-1, steps=2, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), steps=2)
-        tune64 = {"best": best64, "ms_per_2_steps": times64}
-    s64.run(hg.config_2d(t_all=-1, steps=3, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4))
-    s64.upload(rho, u, v, p)
-    i64 = s64.run(hg.config_2d(t_all=-1, steps=args.fp64_steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), stats=True)
-    fp64_rate = m * n * args.fp64_steps / (i64.gpu_ms * 1e-3)
-    s64.close()
-    return {"value": fp64_rate, "unit": "cell-updates/s", "steps": args.fp64_steps,
-            "ms_per_step": i64.gpu_ms / args.fp64_steps,
-            "newton_faces_per_step": i64.newton_faces / args.fp64_steps,
-            "newton_iters_per_face": (i64.newton_iters / i64.newton_faces) if i64.newton_faces else 0.0,
-            "autotune": tune64}
+            "config": {"workload": workload_name(m, n), "form": "fp32 state + learned Newton start",
+                       "grid": [m, n], "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "no flush: 13 planes x 4 B x 16.8M cells = 872 MB per state >> 129 MB L2"},
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "gpu_launches": int(head["launches"]),
+            "clocks": head["clocks"], "forms": forms, "batch": batch}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -650,7 +650,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
     b->halted_kind.assign(b->nprob, 0);
     b->halted_step.assign(b->nprob, 0);
     int halted = 0;
-    unsigned long long nf = 0, ni = 0;
+    unsigned long long nf = 0, ni = 0, nfb = 0;
     for (int p = 0; p < b->nprob; ++p) {
         int q = 0, kind = 0;
         if (hc[p].halted_seq) {
@@ -673,6 +673,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
         }
         nf += hc[p].newton_faces;
         ni += hc[p].newton_iters;
+        nfb += hc[p].newton_fallbacks;
     }
     if (info) {
         memset(info, 0, sizeof(*info));
@@ -685,6 +686,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
         info->halted_problems = halted;
         info->newton_faces = nf;
         info->newton_iters = ni;
+        info->newton_fallbacks = nfb;
     }
     return 0;
 }

@@ -329,6 +329,10 @@ int hydro2d_get_variant(hydro2d_t* h, int* shape)
     return v;
 }
 int hydro2d_set_mlp(hydro2d_t* h, const float* params) { return h->s->set_mlp(params); }
+int hydro2d_conservation(hydro2d_t* h, double hx, double hy, double* sums)
+{
+    return h->s->conservation(hx, hy, sums);
+}
 
 int hydro2d_autotune(hydro2d_t* h, const double* cfg, int ncfg, int steps, float* times_ms)
 {

@@ -66,6 +66,7 @@ public:
     virtual void variant_shape(int v, int* shape) const = 0;
     virtual int autotune(const RunConfig& rc, int steps, float* times_ms) = 0;
     virtual int set_mlp(const float* params) = 0;
+    virtual int conservation(double hx, double hy, double* out4) = 0;
     int m = 0, n = 0, form = 0;
 };
 

@@ -180,6 +180,58 @@ void fill_gas_params(Gas<R>& G, double g, double eps)
     G.eps64 = eps;
 }
 
+// Conservation sums in FP64: mass, x/y momentum and total energy,
+// sum over cells of rho, rho u, rho v, rho E (times the cell area on the
+// host).  Deterministic: block b owns the fixed rows b, b + grid, ..., each
+// block reduces in a fixed tree, and one warp adds the block partials in
+// order, so the result does not depend on scheduling.
+template <typename R>
+__global__ void k_conserve_partial(const R* __restrict__ w, size_t plane, int m, int n, int ld,
+                                   double* __restrict__ partial)
+{
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int j = blockIdx.x; j < m; j += gridDim.x)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const size_t o = (size_t)j * ld + i;
+            const double rho = (double)w[o];
+            s0 += rho;
+            s1 += rho * (double)w[plane + o];
+            s2 += rho * (double)w[2 * plane + o];
+            s3 += rho * (double)w[4 * plane + o];
+        }
+    __shared__ double red[4][32];
+    for (int off = 16; off; off >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, off);
+        s1 += __shfl_down_sync(0xffffffffu, s1, off);
+        s2 += __shfl_down_sync(0xffffffffu, s2, off);
+        s3 += __shfl_down_sync(0xffffffffu, s3, off);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        red[0][wid] = s0;
+        red[1][wid] = s1;
+        red[2][wid] = s2;
+        red[3][wid] = s3;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int q = 0; q < nw; ++q)
+            t += red[threadIdx.x][q];
+        partial[(size_t)blockIdx.x * 4 + threadIdx.x] = t;
+    }
+}
+
+static __global__ void k_conserve_final(const double* __restrict__ partial, int nblocks, double* __restrict__ out)
+{
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int b = 0; b < nblocks; ++b)
+            t += partial[(size_t)b * 4 + threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the solver
 // ---------------------------------------------------------------------------
@@ -340,6 +392,26 @@ public:
     {
         double* dst[5] = {rho, u, v, p, E};
         return download_planes(cur_w, dst);
+    }
+
+    int conservation(double hx, double hy, double* out4) override
+    {
+        constexpr int NB = 512;  // fixed block count: the summation order depends only on the grid
+        double* buf = nullptr;
+        if (!cuda_ok(cudaMalloc(&buf, sizeof(double) * (4 * NB + 4)), "conservation buffer"))
+            return -1;
+        k_conserve_partial<R><<<NB, 256, 0, stream>>>(W(cur_w), plane, m, n, ld, buf);
+        k_conserve_final<<<1, 32, 0, stream>>>(buf, NB, buf + 4 * NB);
+        count_launch(2);
+        double h[4];
+        cudaMemcpyAsync(h, buf + 4 * NB, sizeof(h), cudaMemcpyDeviceToHost, stream);
+        const bool ok = cuda_ok(cudaStreamSynchronize(stream), "conservation sums");
+        cudaFree(buf);
+        if (!ok)
+            return -1;
+        for (int k = 0; k < 4; ++k)
+            out4[k] = h[k] * hx * hy;
+        return 0;
     }
 
     double cfl_hsmax(double gamma, double hmin)
@@ -587,6 +659,7 @@ public:
         info->gpu_ms = ms;
         info->newton_faces = hc.newton_faces;
         info->newton_iters = hc.newton_iters;
+        info->newton_fallbacks = hc.newton_fallbacks;
         cur_w = final_w;
         // slopes are scratch after the run (the reference frees them)
         cur_s = s;

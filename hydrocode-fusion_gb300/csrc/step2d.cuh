@@ -42,7 +42,8 @@ struct Ctl {
     int halt_kind;                 // 1 = abort (that launch is discarded), 2 = stop (kept)
     unsigned long long newton_faces;  // faces that ran the exact solver
     unsigned long long newton_iters;  // Newton iterations summed over those faces
-    unsigned long long pad[4];
+    unsigned long long newton_fallbacks;  // FP32 forms: faces finished by the FP64 Newton iteration
+    unsigned long long pad[3];
 };
 
 template <typename R>
@@ -209,11 +210,12 @@ __device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigne
 // Solve one face given its two sides in the face's normal frame.
 template <typename R>
 __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, const StepArgs<R>& a, FaceOut<R>& o,
-                                          int& iters, bool ydir, R p_start = R(-1))
+                                          int& iters, int& fallback, bool ydir, R p_start = R(-1))
 {
     int code = ifvar_bad(L, Rr, a.G.eps) ? 1 : 0;
     Star<R> S;
     StarInfo st;
+    st.fallback = 0;
     q1d_star(L, Rr, a.G, S, st, p_start);
     R D[4], U[4];
     q1d_derivs(L, Rr, a.G, S, D, U);
@@ -221,6 +223,7 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
         code = 2;
     face_flux<R>(D, U, a.tau, a.htau, a.G, o, ydir);
     iters = st.iters;
+    fallback = st.fallback;
     return code;
 }
 
@@ -378,7 +381,7 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
     // 3. faces, in warp-uniform rounds (every lane of a warp iterates together,
     //    so the learned form can run its warp-collective network)
     constexpr int NFX = (TJ + 1) * TI, NFY = TJ * (TI + 1);
-    int my_iters = 0, my_newton = 0;
+    int my_iters = 0, my_newton = 0, my_fb = 0;
     const int lane = tid & 31;
     for (int fb = tid - lane; fb < NFX + NFY; fb += NT) {
         const int f = fb + lane;
@@ -442,10 +445,12 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
             continue;
         FaceOut<R> o;
         int it;
-        const int code = solve_face<R>(L, Rr, a, o, it, ydir, p_start);
+        int fbk;
+        const int code = solve_face<R>(L, Rr, a, o, it, fbk, ydir, p_start);
         if (it >= 0) {
             my_newton++;
             my_iters += it;
+            my_fb += fbk;
         }
         if (!ydir) {
             report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
@@ -469,10 +474,13 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
         for (int off = 16; off; off >>= 1) {
             my_newton += __shfl_xor_sync(0xffffffffu, my_newton, off);
             my_iters += __shfl_xor_sync(0xffffffffu, my_iters, off);
+            my_fb += __shfl_xor_sync(0xffffffffu, my_fb, off);
         }
         if ((tid & 31) == 0 && my_newton) {
             atomicAdd(&a.ctl->newton_faces, (unsigned long long)my_newton);
             atomicAdd(&a.ctl->newton_iters, (unsigned long long)my_iters);
+            if (my_fb)
+                atomicAdd(&a.ctl->newton_fallbacks, (unsigned long long)my_fb);
         }
     }
     __syncthreads();
@@ -617,7 +625,7 @@ __global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R
     }
     __syncthreads();
 
-    int my_iters = 0, my_newton = 0;
+    int my_iters = 0, my_newton = 0, my_fb = 0;
     for (int f = tid; f < (TA + 1) * TB; f += NT) {
         int fa, lb;
         if (YDIR) { lb = f / (TA + 1); fa = f - lb * (TA + 1); }
@@ -643,10 +651,12 @@ __global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R
         Rr.trho = Rr.tu = Rr.tv = Rr.tp = R(0);
         FaceOut<R> o;
         int it;
-        const int code = solve_face<R>(L, Rr, a, o, it, YDIR != 0);
+        int fbk;
+        const int code = solve_face<R>(L, Rr, a, o, it, fbk, YDIR != 0);
         if (it >= 0) {
             my_newton++;
             my_iters += it;
+            my_fb += fbk;
         }
         int j = YDIR ? cb : ca, i = YDIR ? ca : cb;
         unsigned long long serial = YDIR ? (unsigned long long)j * (n + 1) + i : (unsigned long long)i * (m + 1) + j;
@@ -662,10 +672,13 @@ __global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R
         for (int off = 16; off; off >>= 1) {
             my_newton += __shfl_xor_sync(0xffffffffu, my_newton, off);
             my_iters += __shfl_xor_sync(0xffffffffu, my_iters, off);
+            my_fb += __shfl_xor_sync(0xffffffffu, my_fb, off);
         }
         if ((tid & 31) == 0 && my_newton) {
             atomicAdd(&a.ctl->newton_faces, (unsigned long long)my_newton);
             atomicAdd(&a.ctl->newton_iters, (unsigned long long)my_iters);
+            if (my_fb)
+                atomicAdd(&a.ctl->newton_fallbacks, (unsigned long long)my_fb);
         }
     }
     __syncthreads();

@@ -41,6 +41,7 @@ class RunInfo(ctypes.Structure):
         ("gpu_ms", ctypes.c_double),
         ("newton_faces", ctypes.c_ulonglong),
         ("newton_iters", ctypes.c_ulonglong),
+        ("newton_fallbacks", ctypes.c_ulonglong),
     ]
 
     def as_dict(self):
@@ -58,6 +59,7 @@ class BatchInfo(ctypes.Structure):
         ("halted_problems", ctypes.c_int),
         ("newton_faces", ctypes.c_ulonglong),
         ("newton_iters", ctypes.c_ulonglong),
+        ("newton_fallbacks", ctypes.c_ulonglong),
     ]
 
     def as_dict(self):
@@ -100,6 +102,7 @@ def lib() -> ctypes.CDLL:
     L.hydro2d_get_variant.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.hydro2d_autotune.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     L.hydro2d_set_mlp.argtypes = [ctypes.c_void_p, _fp]
+    L.hydro2d_conservation.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _dp]
     vp = ctypes.c_void_p
     L.hydro_mlp_create.argtypes = [ctypes.POINTER(vp), ctypes.c_ulonglong]
     L.hydro_mlp_destroy.argtypes = [vp]
@@ -230,6 +233,15 @@ class Solver2D:
     def set_mlp(self, params):
         if lib().hydro2d_set_mlp(self._h, np.ascontiguousarray(params, np.float32)) != 0:
             raise RuntimeError(last_error())
+
+    def conservation(self, hx=None, hy=None):
+        """FP64 integrals of mass, x/y momentum and energy of the current state."""
+        hx = 1.0 / self.m if hx is None else hx
+        hy = 1.0 / self.n if hy is None else hy
+        out = np.zeros(4)
+        if lib().hydro2d_conservation(self._h, hx, hy, out) != 0:
+            raise RuntimeError(last_error())
+        return dict(zip(("mass", "mom_x", "mom_y", "energy"), out.tolist()))
 
     def run(self, cfg, split=False, stats=False) -> RunInfo:
         cfg = np.ascontiguousarray(cfg, np.float64)

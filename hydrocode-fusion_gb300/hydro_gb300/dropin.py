@@ -1,6 +1,7 @@
-"""ctypes mirror of the reference's struct cell_var_stru (src/include/var_struc.h:61-74)
-and helpers that call the library's scheme entry points the way the reference's
-drivers do (global config[], caller-owned x-major pointer arrays)."""
+"""The reference-facing call from Python: a ctypes mirror of the reference's
+struct cell_var_stru (src/include/var_struc.h:61-74) and helpers that call the
+library's scheme entry points the way the reference's drivers do (global
+config[], caller-owned x-major pointer arrays of host memory)."""
 import ctypes
 
 import numpy as np
@@ -33,41 +34,52 @@ def _rows(arr2d, keep):
     return ctypes.cast(rows, PP)
 
 
+class Call2D:
+    """Host arrays and arguments of one GRP_solver_2D_[split_]EUL_source call,
+    set up as the 2D driver does (src/hydrocode_2D/hydrocode.c:164-274);
+    call() runs the scheme (host buffers in and out, as a C caller has them)."""
+
+    def __init__(self, lib, rho, u, v, p, gamma, cfg, split=False, plot_times=None, N_MAX=5):
+        m, n = rho.shape
+        self.lib, self.m, self.n, self.split = lib, m, n, split
+        self.cfg = np.array(cfg, np.float64)
+        ntp = 0 if plot_times is None else len(plot_times)
+        self.N_plot0 = ntp + 2
+        self.N_T = min(N_MAX, self.N_plot0)
+        self.time_plot = np.zeros(self.N_plot0)
+        self.time_plot[-1] = cfg[1]
+        if ntp:
+            self.time_plot[1:-1] = plot_times
+        self.data = np.zeros((self.N_T, 5, m, n))
+        d0 = self.data[0]
+        d0[0], d0[1], d0[2], d0[3] = rho, u, v, p
+        E = 0.5 * u * u + p / (gamma - 1.0) / rho
+        E += 0.5 * v * v
+        d0[4] = E
+        self._keep = []
+        self.cvs = (CellVarStru * self.N_T)()
+        for k in range(self.N_T):
+            for idx, name in enumerate(("RHO", "U", "V", "P", "E")):
+                setattr(self.cvs[k], name, _rows(self.data[k, idx], self._keep))
+        self.cpu_time = np.zeros(self.N_T)
+
+    def call(self):
+        conf = config_view(self.lib)
+        conf[:] = self.cfg
+        nplot = ctypes.c_int(self.N_plot0)
+        fn = self.lib.GRP_solver_2D_split_EUL_source if self.split else self.lib.GRP_solver_2D_EUL_source
+        fn.restype = None
+        fn(ctypes.c_int(self.m), ctypes.c_int(self.n), self.cvs, None, None, self.cpu_time.ctypes.data_as(P),
+           ctypes.c_char_p(b"run"), ctypes.c_int(self.N_T), ctypes.byref(nplot), self.time_plot.ctypes.data_as(P))
+        return nplot.value, conf[5]
+
+
 def call_2d(lib, rho, u, v, p, gamma, cfg, split=False, plot_times=None, N_MAX=5):
-    """Run GRP_solver_2D_[split_]EUL_source on x-major (m, n) arrays with the
-    2D driver's set-up (src/hydrocode_2D/hydrocode.c:164-274).  Returns
+    """Run GRP_solver_2D_[split_]EUL_source on x-major (m, n) arrays.  Returns
     (slots[N_T, 5(rho,u,v,p,E), m, n], N_plot, time_plot, config[5])."""
-    m, n = rho.shape
-    ntp = 0 if plot_times is None else len(plot_times)
-    N_plot = ntp + 2
-    N_T = min(N_MAX, N_plot)
-    time_plot = np.zeros(N_plot)
-    time_plot[0] = 0.0
-    time_plot[-1] = cfg[1]
-    if ntp:
-        time_plot[1:-1] = plot_times
-    data = np.zeros((N_T, 5, m, n))
-    data[0, 0], data[0, 1], data[0, 2], data[0, 3] = rho, u, v, p
-    E = 0.5 * u * u + p / (gamma - 1.0) / rho
-    E += 0.5 * v * v
-    data[0, 4] = E
-    keep = []
-    cvs = (CellVarStru * N_T)()
-    for k in range(N_T):
-        cvs[k].RHO = _rows(data[k, 0], keep)
-        cvs[k].U = _rows(data[k, 1], keep)
-        cvs[k].V = _rows(data[k, 2], keep)
-        cvs[k].P = _rows(data[k, 3], keep)
-        cvs[k].E = _rows(data[k, 4], keep)
-    conf = config_view(lib)
-    conf[:] = cfg
-    cpu_time = np.zeros(N_T)
-    nplot = ctypes.c_int(N_plot)
-    fn = lib.GRP_solver_2D_split_EUL_source if split else lib.GRP_solver_2D_EUL_source
-    fn.restype = None
-    fn(ctypes.c_int(m), ctypes.c_int(n), cvs, None, None, cpu_time.ctypes.data_as(P), ctypes.c_char_p(b"test"),
-       ctypes.c_int(N_T), ctypes.byref(nplot), time_plot.ctypes.data_as(P))
-    return data, nplot.value, time_plot, conf[5]
+    c = Call2D(lib, rho, u, v, p, gamma, cfg, split, plot_times, N_MAX)
+    nplot, k_out = c.call()
+    return c.data, nplot, c.time_plot, k_out
 
 
 def call_1d(lib, rho, u, p, gamma, cfg, order, plot_times=None, N_MAX=1000):

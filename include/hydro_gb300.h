@@ -95,6 +95,7 @@ typedef struct {
     double tau;           /* last time step */
     double gpu_ms;        /* device time of the time loop (CUDA events) */
     unsigned long long newton_faces, newton_iters;  /* exact-solver statistics (when enabled) */
+    unsigned long long newton_fallbacks;            /* FP32 forms: faces finished by the FP64 iteration */
 } hydro_run_info;
 
 /* Create a solver for an m (x) by n (y) grid in the given form. 0 on success. */
@@ -166,6 +167,9 @@ int hydro_mlp_gradient(hydro_mlp_t *h, const float *X, const float *Y, int n, fl
 int hydro_mlp_predict(hydro_mlp_t *h, const float *X, int n, float *Y);
 /* The device feature map of states rhoL,uL,pL,rhoR,uR,pR (rows of 6). */
 int hydro_mlp_features(const double *states, int n, double gamma, float *X);
+/* Conservation integrals of the current state, summed in FP64 in a fixed
+ * order (deterministic): sums[4] = h_x h_y * sum of rho, rho u, rho v, rho E. */
+int hydro2d_conservation(hydro2d_t *h, double hx, double hy, double *sums);
 /* Install network parameters into a solver of the HYDRO_FORM_FP32_LEARNED form. */
 int hydro2d_set_mlp(hydro2d_t *h, const float *params);
 /* ---- batched problems (no reference counterpart) --------------------------
@@ -188,7 +192,7 @@ typedef struct {
     int graphed;              /* 1 if the time loop ran as one captured CUDA graph */
     int steps, tiles;         /* steps run; tiles per step over all problems */
     int halted_problems;      /* problems that stopped or aborted early */
-    unsigned long long newton_faces, newton_iters; /* with stats = 1 */
+    unsigned long long newton_faces, newton_iters, newton_fallbacks; /* with stats = 1 */
 } hydro_batch_info;
 int hydro_batch_create(hydro_batch_t **out, int nprob, const int *m, const int *n);
 void hydro_batch_destroy(hydro_batch_t *b);

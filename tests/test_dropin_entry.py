@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from cvstruct import call_1d, call_2d
+from hydro_gb300.dropin import call_1d, call_2d
 from helpers import rel_l1
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")

@@ -92,6 +92,11 @@ def test_learned_guess_saves_newton_iterations(gpu_lib):
     it_learned = il.newton_iters / il.newton_faces
     assert ip.newton_faces > 0.5 * 2 * m * n * 20  # most faces run the exact solver here
     assert it_learned < it_plain, (it_plain, it_learned)
+    # v is a small perturbation field here (|v| ~ 1e-2): FP32 rounding alone
+    # gives it a relative L1 of order 1e-4, so v is held to the plain FP32
+    # form's own error; the O(1) fields to 1e-5
     for f in ("rho", "u", "v", "p"):
         rel = np.abs(learned[f] - ref[f]).sum() / np.abs(ref[f]).sum()
-        assert rel <= 1e-5, (f, rel)
+        rel_plain = np.abs(plain[f] - ref[f]).sum() / np.abs(ref[f]).sum()
+        bound = 1.25 * rel_plain + 1e-7 if f == "v" else 1e-5
+        assert rel <= bound, (f, rel, rel_plain)
