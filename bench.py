@@ -143,12 +143,13 @@ def rel_l1(a, b):
     return float(np.abs(a - b).sum() / d) if d > 0 else float(np.abs(a - b).sum())
 
 
-def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dist=None):
-    """Tune, warm up, then time K steps of one form from the initial state.
-    Returns a dict with the rate, the final state and statistics."""
+def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dist=None, bnd=-4):
+    """Tune, warm up, then time K steps of one form from the initial state
+    (boundary code bnd on all sides).  Returns a dict with the rate, the final
+    state and statistics."""
     rho, u, v, p = state
-    cfgK = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
-    cfgW = hg.config_2d(t_all=-1, steps=W, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
+    cfgK = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd)
+    cfgW = hg.config_2d(t_all=-1, steps=W, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd)
     s = hg.Solver2D(m, n, form)
     res = {}
     try:
@@ -191,7 +192,7 @@ def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dis
         res["state"] = s.download()
         if stats_steps > 0:
             s.upload(rho, u, v, p)
-            i2 = s.run(hg.config_2d(t_all=-1, steps=stats_steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4), stats=True)
+            i2 = s.run(hg.config_2d(t_all=-1, steps=stats_steps, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd), stats=True)
             faces = 2.0 * m * n * stats_steps
             res["newton"] = {"steps": stats_steps, "exact_solves_per_face": i2.newton_faces / faces,
                              "iters_per_exact_solve": (i2.newton_iters / i2.newton_faces) if i2.newton_faces else 0.0,
@@ -209,11 +210,24 @@ def e2e_run(hg, state, m, n, K):
     rho, u, v, p = state
     cfg = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4, form=hg.FORM_FP32_LEARNED)
     c = Call2D(hg.lib(), rho, u, v, p, 1.4, cfg, N_MAX=2)
-    l0 = hg.kernel_launches()
-    t0 = time.perf_counter()
-    nplot, k_out = c.call()
-    wall = time.perf_counter() - t0
-    launches = hg.kernel_launches() - l0
+    # the scheme call reports on stdout as the reference's does: keep that
+    # text out of this program's one JSON line
+    import ctypes
+
+    sys.stdout.flush()
+    saved, devnull = os.dup(1), os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    try:
+        l0 = hg.kernel_launches()
+        t0 = time.perf_counter()
+        nplot, k_out = c.call()
+        wall = time.perf_counter() - t0
+        launches = hg.kernel_launches() - l0
+        ctypes.CDLL(None).fflush(None)
+    finally:
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(devnull)
     plane_bytes = 8 * m * n
     return {"value": m * n * K / wall, "unit": UNIT, "h2d_bytes_per_step": 5 * plane_bytes / K,
             "d2h_bytes_per_step": 5 * plane_bytes / K, "wall_s": wall, "k_out": int(k_out), "launches": int(launches),
@@ -262,6 +276,29 @@ def batch_run(hg, count, steps, tune_steps, l1_sample):
             "halted_problems": info.halted_problems, "per_problem_l1_vs_fp64": l1}
 
 
+def shear_suite(hg, m, n, K, W, tune, stats_steps):
+    """Periodic shear layer (rho = 2, u = +0.5 inside |y - 1/2| < 1/4, else
+    rho = 1, u = -0.5; p = 2.5; v = 0.01 sin(4 pi x) + seeded noise 1e-3):
+    Newton-heavy data, where most faces need the exact Riemann solver.  The
+    FP32 forms are timed and compared with the FP64 form."""
+    from hydro_gb300 import cases
+
+    state = cases.shear_layer(m, n, seed=1)
+    res = {}
+    for key, form in (("fp32_learned", hg.FORM_FP32_LEARNED), ("fp32", hg.FORM_FP32), ("fp64", hg.FORM_FP64)):
+        res[key] = timed_form(hg, form, state, m, n, K, W, tune, stats_steps, bnd=-7)
+    out = {"workload": f"2D unsplit GRP, {m}x{n} periodic shear layer (seed 1), gamma 1.4, CFL 0.45", "steps": K}
+    for key in ("fp32_learned", "fp32", "fp64"):
+        r = res[key]
+        out[key] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "kernel_variant": r["kernel_variant"],
+                    "newton": r.get("newton"), "halted": r["halted"]}
+        if key != "fp64":
+            out[key]["l1_vs_fp64"] = {f: rel_l1(r["state"][f], res["fp64"]["state"][f]) for f in ("rho", "u", "v", "p")}
+    out["speedup_learned_over_fp32"] = res["fp32_learned"]["value"] / res["fp32"]["value"]
+    out["speedup_learned_over_fp64"] = res["fp32_learned"]["value"] / res["fp64"]["value"]
+    return out
+
+
 def reference_arm(args, m, n, rank):
     if rank != 0:
         return
@@ -296,6 +333,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the kernel-variant autotuners")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-shear", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=300)
     args = ap.parse_args()
@@ -343,11 +381,13 @@ def main():
     peak, peak_kind = peaks()
     ms = head["ms_per_step"]
     achieved = BYTES_PER_CELL_F32 * m * n / (ms * 1e-3) / 1e9
-    tpc = traffic_per_cell("k_step_unsplit<float,learned>")
+    kv = head["kernel_variant"]
+    kname = "%s<float,%dx%d,%d,learned>" % ("k_step_tma" if kv.get("tma") else "k_step_unsplit", kv["tile_x"],
+                                             kv["tile_y"], kv["threads"])
+    tpc = traffic_per_cell(kname)
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": tpc * m * n if tpc else None, "peak_source": peak_kind,
-            "kernel": "k_step_unsplit<float, learned> (one launch per step)",
-            "algorithmic_bytes_per_launch": BYTES_PER_CELL_F32 * m * n}
+            "kernel": kname + " (one launch per step)", "algorithmic_bytes_per_launch": BYTES_PER_CELL_F32 * m * n}
 
     forms = {
         "fp32_learned": summary(head, "f32") | {"l1_vs_fp64": accuracy(head)},
@@ -364,6 +404,7 @@ def main():
 
     e2e = None if args.no_e2e else e2e_run(hg, state, m, n, K)
     batch = None if args.no_batch else batch_run(hg, args.batch_count, args.batch_steps, 5, 8)
+    shear = None if args.no_shear else shear_suite(hg, m, n, K, W, tune, args.stats_steps)
 
     cpu = None
     if not args.no_cpu:
@@ -379,7 +420,7 @@ def main():
                        "grid": [m, n], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "no flush: 13 planes x 4 B x 16.8M cells = 872 MB per state >> 129 MB L2"},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "gpu_launches": int(head["launches"]),
-            "clocks": head["clocks"], "forms": forms, "batch": batch}
+            "clocks": head["clocks"], "forms": forms, "shear": shear, "batch": batch}
     print(json.dumps(line), flush=True)
 
 

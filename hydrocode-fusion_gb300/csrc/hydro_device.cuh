@@ -359,15 +359,30 @@ __device__ __noinline__ void q1d_star_exact(const Side<R>& L, const Side<R>& Rr,
 
 // Star state of linear_GRP_solver_Edir_Q1D (:92-134) with atc = eps:
 // uniform pairs (dist < eps) take the averaged state, all others the exact solver.
+// The uniform-pair test of q1d_star (the acoustic case), on its own: used to
+// sort faces before solving them; q1d_star makes the decision again itself.
 template <typename R>
+__device__ __forceinline__ bool face_uniform(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G)
+{
+    const R rho_L = L.rho, rho_R = Rr.rho, u_L = L.u, u_R = Rr.u, p_L = L.p, p_R = Rr.p;
+    R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
+    return StarPolicy<R>::uniform(dist, rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R), G);
+}
+
+// KNOWN: 0 = make the uniform-pair decision here; 1 / 2 = the caller has
+// already made it with face_uniform (1 uniform, 2 not), so only that branch
+// is compiled into the caller.
+template <typename R, int KNOWN = 0>
 __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
                                          StarInfo& st, R p_start = R(-1))
 {
     const R rho_L = L.rho, rho_R = Rr.rho, u_L = L.u, u_R = Rr.u, p_L = L.p, p_R = Rr.p;
     S.c_L = M<R>::sqrt_(G.g * p_L / rho_L);
     S.c_R = M<R>::sqrt_(G.g * p_R / rho_R);
-    R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
-    S.acoustic = StarPolicy<R>::uniform(dist, rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R), G);
+    if constexpr (KNOWN == 0)
+        S.acoustic = face_uniform<R>(L, Rr, G);
+    else
+        S.acoustic = (KNOWN == 1);
     if (S.acoustic) {
         S.u_star = R(0.5) * (u_R + u_L);
         S.p_star = R(0.5) * (p_R + p_L);

@@ -14,7 +14,10 @@
 
 #include <stdlib.h>
 
+#include <string>
 #include <vector>
+
+#include <cudaTypedefs.h>
 
 #include "solver2d.h"
 #include "step2d.cuh"
@@ -24,11 +27,16 @@ namespace hydro {
 // Compiled configurations of the unsplit step kernel (tile TJ x TI cells,
 // NT threads, at least MINB resident CTAs per SM requested from ptxas).  The
 // autotuner (Solver2D::autotune) times them on the actual problem.
+// tma = 1: the persistent TMA-staged kernel (k_step_tma), launched with
+// occ CTAs per SM; tma = 0: one CTA per tile (k_step_unsplit).
 template <typename R>
 struct StepVariant {
     int TJ, TI, NT, MINB;
     size_t smem;
     const void* kern;
+    int tma = 0;
+    int occ = 0;
+    StepMaps maps[2];  // tma: descriptors of the two state buffers
 };
 
 template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false>
@@ -36,7 +44,14 @@ StepVariant<R> step_variant()
 {
     return StepVariant<R>{TJ, TI, NT, MINB,
                           LEARNED ? UnsplitSmem<R, TJ, TI>::bytes_learned : UnsplitSmem<R, TJ, TI>::bytes,
-                          (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED>};
+                          (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED>, 0, 0, {}};
+}
+
+template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false>
+StepVariant<R> tma_variant()
+{
+    return StepVariant<R>{TJ, TI, NT, MINB, TmaSmem<R, TJ, TI, LEARNED>::bytes,
+                          (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED>, 1, 0, {}};
 }
 
 template <typename R> struct Variants;
@@ -44,7 +59,8 @@ template <> struct Variants<double> {
     static std::vector<StepVariant<double>> all(bool)
     {
         return {step_variant<double, 16, 16, 256, 1>(), step_variant<double, 16, 16, 256, 3>(),
-                step_variant<double, 8, 16, 128, 4>(), step_variant<double, 32, 16, 512, 1>()};
+                step_variant<double, 8, 16, 128, 4>(), step_variant<double, 32, 16, 512, 1>(),
+                tma_variant<double, 16, 16, 256, 1>(),  tma_variant<double, 32, 16, 512, 1>()};
     }
     static constexpr int SJ = 16, SI = 32, SNT = 256;  // split sweeps
 };
@@ -53,11 +69,14 @@ template <> struct Variants<float> {
     {
         if (learned)
             return {step_variant<float, 32, 32, 512, 1, true>(), step_variant<float, 16, 32, 512, 1, true>(),
-                    step_variant<float, 16, 16, 256, 2, true>()};
+                    step_variant<float, 16, 32, 512, 2, true>(), step_variant<float, 16, 16, 256, 2, true>(),
+                    step_variant<float, 16, 16, 256, 3, true>(), tma_variant<float, 32, 32, 512, 1, true>(),
+                    tma_variant<float, 16, 32, 512, 1, true>()};
         return {step_variant<float, 16, 32, 512, 1>(), step_variant<float, 16, 16, 256, 2>(),
                 step_variant<float, 16, 16, 256, 3>(), step_variant<float, 16, 16, 256, 4>(),
                 step_variant<float, 8, 32, 256, 3>(),  step_variant<float, 32, 32, 512, 1>(),
-                step_variant<float, 16, 32, 512, 2>()};
+                step_variant<float, 16, 32, 512, 2>(), tma_variant<float, 32, 32, 512, 1>(),
+                tma_variant<float, 16, 32, 512, 1>()};
     }
     static constexpr int SJ = 16, SI = 32, SNT = 256;
 };
@@ -253,6 +272,37 @@ public:
     R* Sx(int b) { return W(b) + 5 * plane; }
     R* Ty(int b) { return W(b) + 9 * plane; }
 
+    // Tensor map over `planes` consecutive pitched planes starting at base
+    // (dims n x m x planes, innermost n), box bw x bh x planes.
+    bool encode_planes(CUtensorMap* map, R* base, int planes, int bw, int bh)
+    {
+        static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+        if (!encode) {
+            cudaDriverEntryPointQueryResult q;
+            void* fn = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                    cudaSuccess ||
+                q != cudaDriverEntryPointSuccess || !fn) {
+                set_error("cuTensorMapEncodeTiled is not available");
+                return false;
+            }
+            encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        }
+        const cuuint64_t dims[3] = {(cuuint64_t)n, (cuuint64_t)m, (cuuint64_t)planes};
+        const cuuint64_t strides[2] = {(cuuint64_t)ld * sizeof(R), (cuuint64_t)plane * sizeof(R)};
+        const cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, (cuuint32_t)planes};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const CUresult r = encode(map, sizeof(R) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                                  3, (void*)base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            set_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+            return false;
+        }
+        return true;
+    }
+
     int init(int m_, int n_, int form_)
     {
         m = m_;
@@ -279,7 +329,14 @@ public:
                 !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network"))
                 return -1;
         }
+        int smem_optin = 0;
+        cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         for (auto& v : variants) {
+            if ((int)v.smem > smem_optin) {  // too large for this device: dropped below
+                v.tma = 1;
+                v.occ = 0;
+                continue;
+            }
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem),
                          "smem attr"))
                 return -1;
@@ -287,6 +344,27 @@ public:
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
                          "carveout attr"))
                 return -1;
+            if (v.tma) {
+                if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v.occ, v.kern, v.NT, v.smem),
+                             "occupancy"))
+                    return -1;
+                if (v.occ < 1)
+                    continue;  // does not fit on an SM: dropped below
+                // descriptors of both state buffers: box of 5 value planes x (TJ+4) rows, 8 slope
+                // planes x (TJ+2) rows, TI + 2X columns
+                const int bw = v.TI + 2 * (16 / (int)sizeof(R));
+                for (int b = 0; b < 2; ++b)
+                    if (!encode_planes(&v.maps[b].vals, W(b), 5, bw, v.TJ + 4) ||
+                        !encode_planes(&v.maps[b].slopes, W(b) + 5 * plane, 8, bw, v.TJ + 2))
+                        return -1;
+            }
+        }
+        {
+            std::vector<StepVariant<R>> keep;
+            for (auto& v : variants)
+                if (!v.tma || v.occ >= 1)
+                    keep.push_back(v);
+            variants.swap(keep);
         }
         size_t smem_x = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SJ, TS::SI);
         size_t smem_y = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SI, TS::SJ);
@@ -450,6 +528,7 @@ public:
         shape[1] = s.TI;
         shape[2] = s.NT;
         shape[3] = s.MINB;
+        shape[4] = s.tma;
     }
 
     // Times every variant on `steps` steps of the uploaded state (restored
@@ -473,11 +552,8 @@ public:
             cur_w = w0;
             hydro_run_info info;
             int nt;
-            if (run(r2, 0, 0, tp, 2, 2, nullptr, &info, &nt)) {
-                cudaFree(backup);
-                return -1;
-            }
-            float ms = (float)info.gpu_ms;
+            // a variant that fails to run is timed as infinitely slow
+            float ms = run(r2, 0, 0, tp, 2, 2, nullptr, &info, &nt) ? 3e38f : (float)info.gpu_ms;
             if (times_ms)
                 times_ms[v] = ms;
             if (ms < best_ms) {
@@ -561,7 +637,11 @@ public:
         std::vector<int> wbuf_before(plan.sweeps.size() + 1);
 
         cudaEventRecord(ev0, stream);
-        int w = cur_w, s = cur_s, t = cur_t;
+        // slopes are scratch between runs (the first limiting of a run ignores
+        // them), so they restart in the state's own buffer, as the TMA boxes expect
+        int w = cur_w, s = cur_w, t = cur_w;
+        const int ntiles_u = ((n + V.TI - 1) / V.TI) * ((m + V.TJ - 1) / V.TJ);
+        const int grid_tma = V.tma ? (ntiles_u < sms * V.occ ? ntiles_u : sms * V.occ) : 0;
         for (size_t q = 0; q < plan.sweeps.size(); ++q) {
             const SweepRec& r = plan.sweeps[q];
             int seq = (int)q + 1;
@@ -589,9 +669,18 @@ public:
             if (r.dir == 0) {
                 a.src_s = Sx(s); a.dst_s = Sx(s ^ 1);
                 a.src_t = Ty(t); a.dst_t = Ty(t ^ 1);
-                void* args[] = {(void*)&a};
-                if (!cuda_ok(cudaLaunchKernel(V.kern, gu, dim3(V.NT), args, V.smem, stream), "step launch"))
-                    return -1;
+                if (V.tma) {
+                    // the boxes read the state buffer w, whose slope planes are s = t = w here
+                    StepMaps mp = V.maps[w];
+                    void* args[] = {(void*)&a, (void*)&mp};
+                    if (!cuda_ok(cudaLaunchKernel(V.kern, dim3(grid_tma), dim3(V.NT), args, V.smem, stream),
+                                 "step launch"))
+                        return -1;
+                } else {
+                    void* args[] = {(void*)&a};
+                    if (!cuda_ok(cudaLaunchKernel(V.kern, gu, dim3(V.NT), args, V.smem, stream), "step launch"))
+                        return -1;
+                }
                 s ^= 1;
                 t ^= 1;
             } else if (r.dir == 1) {
@@ -617,6 +706,10 @@ public:
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev0, ev1);
         (void)wbuf_at_seq0;
+        if (hc.wait_err) {
+            set_error("a bounded TMA wait in the step kernel gave up; the run is invalid");
+            return -1;
+        }
 
         // resolve the outcome
         int nsw = (int)plan.sweeps.size();

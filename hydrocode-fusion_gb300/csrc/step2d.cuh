@@ -29,8 +29,11 @@
 // the way the reference does (abort = discard the step, stop = keep it).
 #pragma once
 
+#include <type_traits>
+
 #include "hydro_device.cuh"
 #include "learned.cuh"
+#include "tma.cuh"
 
 namespace hydro {
 
@@ -43,7 +46,9 @@ struct Ctl {
     unsigned long long newton_faces;  // faces that ran the exact solver
     unsigned long long newton_iters;  // Newton iterations summed over those faces
     unsigned long long newton_fallbacks;  // FP32 forms: faces finished by the FP64 Newton iteration
-    unsigned long long pad[3];
+    unsigned int wait_err;                // a bounded wait in a kernel gave up (the launch is invalid)
+    unsigned int pad32;
+    unsigned long long pad[2];
 };
 
 template <typename R>
@@ -207,8 +212,9 @@ __device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigne
         atomicMax(&ctl->key[slot][dir], ((serial + 1ull) << 2) | (unsigned long long)code);
 }
 
-// Solve one face given its two sides in the face's normal frame.
-template <typename R>
+// Solve one face given its two sides in the face's normal frame (KNOWN as in
+// q1d_star: whether the uniform-pair decision has already been made).
+template <typename R, int KNOWN = 0>
 __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, const StepArgs<R>& a, FaceOut<R>& o,
                                           int& iters, int& fallback, bool ydir, R p_start = R(-1))
 {
@@ -216,7 +222,7 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
     Star<R> S;
     StarInfo st;
     st.fallback = 0;
-    q1d_star(L, Rr, a.G, S, st, p_start);
+    q1d_star<R, KNOWN>(L, Rr, a.G, S, st, p_start);
     R D[4], U[4];
     q1d_derivs(L, Rr, a.G, S, D, U);
     if (star_dire_check2(U, D, a.G.eps))
@@ -281,40 +287,73 @@ struct UnsplitSmem {
     static constexpr int nS = 8 * SJ * SI;
     static constexpr int nFX = 8 * (TJ + 1) * TI;
     static constexpr int nFY = 8 * TJ * (TI + 1);
-    static constexpr size_t bytes = sizeof(R) * (size_t)(nW + nS + nFX + nFY);
-    // the learned form appends the network image
-    static constexpr size_t bytes_learned = (bytes + 15) / 16 * 16 + sizeof(MlpShared);
+    static constexpr int nQ = (TJ + 1) * TI + TJ * (TI + 1);  // queue of faces for the exact solver
+    static constexpr size_t bytes_f = sizeof(R) * (size_t)(nW + nS + nFX + nFY);
+    static constexpr size_t bytes = bytes_f + (2 * (size_t)nQ + 15) / 16 * 16;
+    // the learned form appends the starting pressures of the queued faces and the network image
+    static constexpr size_t p_off = (bytes + 15) / 16 * 16;
+    static constexpr size_t mlp_off = p_off + 4 * (size_t)nQ;
+    static constexpr size_t bytes_learned = mlp_off + sizeof(MlpShared);
+};
+
+// Shared-memory stage of one tile's TMA copy: box A = 5 value planes
+// (rho u v p E) x rows J0-2 .. J0+TJ+1 x columns I0-X .. I0-X+BW-1, box B = 8
+// previous-slope planes x rows J0-1 .. J0+TJ x the same columns.  X is 16
+// bytes of elements, so every copy starts on a 16-byte column boundary.
+template <typename R, int TJ, int TI>
+struct StageLayout {
+    static constexpr int X = 16 / (int)sizeof(R);
+    static constexpr int BW = TI + 2 * X;
+    static constexpr int AJ = TJ + 4, BJ = TJ + 2;
+    static constexpr size_t a_bytes = sizeof(R) * 5 * AJ * BW;
+    static constexpr size_t b_bytes = sizeof(R) * 8 * BJ * BW;
+    static constexpr size_t a_off = 0, b_off = (a_bytes + 127) / 128 * 128;
+    static constexpr size_t bytes = b_off + (b_bytes + 127) / 128 * 128;  // one stage
 };
 
 // One TJ x TI tile (cells i in [I0, I0+TI), j in [J0, J0+TJ)) of the unsplit
-// step, computed by a block of NT threads; used by the one-problem kernel
-// below and by the batched persistent kernel.  Ends with a block barrier, so
-// the shared memory can be reused for the next tile at once.
-template <typename R, int TJ, int TI, int NT, bool LEARNED>
-__device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0, const int J0, unsigned char* smem_raw,
-                                             const MlpShared& Mlp)
+// step, computed by a block of NT threads.  Ends with a block barrier, so the
+// shared memory can be reused for the next tile at once.
+//   STAGED = false: the tile gathers its values (with boundary ghosts) from
+//     global memory into W (pitch TI+4) itself; used by the one-problem kernel
+//     k_step_unsplit and by the batched kernels.
+//   STAGED = true: a TMA copy has already placed the 5 value planes (rows
+//     J0-2.., columns I0-X.., pitch BW) at W and the 8 previous-slope planes
+//     (rows J0-1.., same columns) at B; only the ghost cells of tiles at the
+//     domain edge are gathered.  FX may alias B (B is dead after phase 2).
+template <typename R, int TJ, int TI, int NT, bool LEARNED, bool STAGED>
+__device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, const int J0, R* __restrict__ W,
+                                          const R* B, R* __restrict__ S, R* FX, R* __restrict__ FY,
+                                          unsigned short* __restrict__ Q, float* __restrict__ P,
+                                          const MlpShared& Mlp)
 {
     using SM = UnsplitSmem<R, TJ, TI>;
-    R* W = reinterpret_cast<R*>(smem_raw);
-    R* S = W + SM::nW;
-    R* FX = S + SM::nS;
-    R* FY = FX + SM::nFX;
+    using SL = StageLayout<R, TJ, TI>;
     const int tid = threadIdx.x;
     const int m = a.m, n = a.n, slot = a.seq % 3;
-    constexpr int WJ = SM::WJ, WI = SM::WI, SJ = SM::SJ, SI = SM::SI;
-#define Wx(k, lj, li) W[((k) * WJ + (lj)) * WI + (li)]
+    constexpr int WJ = SM::WJ, SJ = SM::SJ, SI = SM::SI;
+    // value (lj, li) = cell (J0-2+lj, I0-2+li)
+    constexpr int WP = STAGED ? SL::BW : SM::WI;
+    constexpr int WO = STAGED ? SL::X - 2 : 0;
+#define Wx(k, lj, li) W[((k) * WJ + (lj)) * WP + (li) + WO]
 #define Sx(k, sj, si) S[((k) * SJ + (sj)) * SI + (si)]
 #define FXx(k, fj, fi) FX[((k) * (TJ + 1) + (fj)) * TI + (fi)]
 #define FYx(k, gj, gi) FY[((k) * TJ + (gj)) * (TI + 1) + (gi)]
 
-    // 1. values with a 2-cell halo
-    for (int idx = tid; idx < WJ * WI; idx += NT) {
-        int lj = idx / WI, li = idx - lj * WI;
-        R w[4];
-        load_prims(a, J0 - 2 + lj, I0 - 2 + li, w);
+    // 1. values with a 2-cell halo (staged: only the ghosts of edge tiles)
+    constexpr int WI = SM::WI;
+    if (!STAGED || J0 < 2 || I0 < 2 || J0 + TJ + 2 > m || I0 + TI + 2 > n) {
+        for (int idx = tid; idx < WJ * WI; idx += NT) {
+            int lj = idx / WI, li = idx - lj * WI;
+            const int j = J0 - 2 + lj, i = I0 - 2 + li;
+            if (STAGED && j >= 0 && j < m && i >= 0 && i < n)
+                continue;
+            R w[4];
+            load_prims(a, j, i, w);
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            Wx(k, lj, li) = w[k];
+            for (int k = 0; k < 4; ++k)
+                Wx(k, lj, li) = w[k];
+        }
     }
     __syncthreads();
 
@@ -324,13 +363,21 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
         if ((sj == 0 || sj == SJ - 1) && (si == 0 || si == SI - 1))
             continue;
         int j = J0 - 1 + sj, i = I0 - 1 + si;
+        const bool inside = STAGED && j >= 0 && j < m && i >= 0 && i < n;
         size_t o = slope_index(a, j, i);
+        // staged previous slopes: plane k at B[(k * BJ + sj) * BW + si - 1 + X]
+        const R* bs = STAGED ? B + sj * SL::BW + si - 1 + SL::X : nullptr;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
+            R ps = R(0), pt = R(0);
+            if (a.find_x)
+                ps = inside ? bs[k * SL::BJ * SL::BW] : a.src_s[k * a.plane + o];
+            if (a.find_y)
+                pt = inside ? bs[(4 + k) * SL::BJ * SL::BW] : a.src_t[k * a.plane + o];
             R sx = limit(Wx(k, sj, si + 1), Wx(k, sj + 1, si + 1), Wx(k, sj + 2, si + 1), a.hx, a.inv_hx, a.pow2_x,
-                         a.alpha, a.find_x, a.find_x ? a.src_s[k * a.plane + o] : R(0));
+                         a.alpha, a.find_x, ps);
             R sy = limit(Wx(k, sj + 1, si), Wx(k, sj + 1, si + 1), Wx(k, sj + 1, si + 2), a.hy, a.inv_hy, a.pow2_y,
-                         a.alpha, a.find_y, a.find_y ? a.src_t[k * a.plane + o] : R(0));
+                         a.alpha, a.find_y, pt);
             Sx(k, sj, si) = sx;
             Sx(4 + k, sj, si) = sy;
         }
@@ -378,22 +425,24 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
     }
     __syncthreads();
 
-    // 3. faces, in warp-uniform rounds (every lane of a warp iterates together,
-    //    so the learned form can run its warp-collective network)
-    constexpr int NFX = (TJ + 1) * TI, NFY = TJ * (TI + 1);
+    // 3. faces, in two passes.  Pass A reconstructs every face: a pair within
+    //    the uniform threshold (the acoustic case of the GRP solver) is
+    //    solved at once, any other face goes to a shared-memory queue.  Pass B
+    //    solves the queued faces 32 to a warp, so the exact Riemann solver
+    //    (and the learned network) run on full warps instead of on the one or
+    //    two lanes of a warp that need them while the rest idle.  Every face is
+    //    computed by the same solve_face in either pass, so the split changes
+    //    no result.
+    constexpr int NFX = (TJ + 1) * TI, NFY = TJ * (TI + 1), NF = NFX + NFY;
     int my_iters = 0, my_newton = 0, my_fb = 0;
     const int lane = tid & 31;
-    for (int fb = tid - lane; fb < NFX + NFY; fb += NT) {
-        const int f = fb + lane;
-        const bool ydir = f >= NFX;
-        bool active = f < NFX + NFY;
-        int lj = 0, li = 0, j = 0, i = 0;
-        Side<R> L, Rr;
-        if (active && !ydir) {
+    // sides of face f (x-faces first, then y-faces) in the face's normal frame;
+    // false when the face lies outside the domain
+    auto sides = [&](int f, Side<R>& L, Side<R>& Rr, int& lj, int& li, int& j, int& i) -> bool {
+        if (f < NFX) {
             const int fj = f / TI, fi = f - fj * TI;
             lj = fj; li = fi;
             j = J0 + fj; i = I0 + fi;
-            active = !(j > m || i >= n);
             // left cell (j-1): slopes at (fj, fi+1), values at (fj+1, fi+2)
             L.drho = Sx(0, fj, fi + 1); L.du = Sx(1, fj, fi + 1); L.dv = Sx(2, fj, fi + 1); L.dp = Sx(3, fj, fi + 1);
             L.trho = Sx(4, fj, fi + 1); L.tu = Sx(5, fj, fi + 1); L.tv = Sx(6, fj, fi + 1); L.tp = Sx(7, fj, fi + 1);
@@ -407,46 +456,45 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
             Rr.u = Wx(1, fj + 2, fi + 2) - a.hhx * Rr.du;
             Rr.v = Wx(2, fj + 2, fi + 2) - a.hhx * Rr.dv;
             Rr.p = Wx(3, fj + 2, fi + 2) - a.hhx * Rr.dp;
-        } else if (active) {
-            const int g = f - NFX;
-            const int gj = g / (TI + 1), gi = g - gj * (TI + 1);
-            lj = gj; li = gi;
-            j = J0 + gj; i = I0 + gi;
-            active = !(j >= m || i > n);
-            // lower cell (i-1): slopes at (gj+1, gi), values at (gj+2, gi+1); rotated to the +y normal frame:
-            // normal velocity v, tangential -u; normal derivatives are the y-slopes, tangential the negated x-slopes
-            {
-                R t0 = Sx(4, gj + 1, gi), t1 = Sx(5, gj + 1, gi), t2 = Sx(6, gj + 1, gi), t3 = Sx(7, gj + 1, gi);
-                R s0 = Sx(0, gj + 1, gi), s1 = Sx(1, gj + 1, gi), s2 = Sx(2, gj + 1, gi), s3 = Sx(3, gj + 1, gi);
-                R rr = Wx(0, gj + 2, gi + 1) + a.hhy * t0;
-                R uu = Wx(1, gj + 2, gi + 1) + a.hhy * t1;
-                R vv = Wx(2, gj + 2, gi + 1) + a.hhy * t2;
-                R pp = Wx(3, gj + 2, gi + 1) + a.hhy * t3;
-                L.rho = rr; L.u = vv; L.v = -uu; L.p = pp;
-                L.drho = t0; L.du = t2; L.dv = -t1; L.dp = t3;
-                L.trho = -s0; L.tu = -s2; L.tv = s1; L.tp = -s3;
-            }
-            {
-                R t0 = Sx(4, gj + 1, gi + 1), t1 = Sx(5, gj + 1, gi + 1), t2 = Sx(6, gj + 1, gi + 1), t3 = Sx(7, gj + 1, gi + 1);
-                R s0 = Sx(0, gj + 1, gi + 1), s1 = Sx(1, gj + 1, gi + 1), s2 = Sx(2, gj + 1, gi + 1), s3 = Sx(3, gj + 1, gi + 1);
-                R rr = Wx(0, gj + 2, gi + 2) - a.hhy * t0;
-                R uu = Wx(1, gj + 2, gi + 2) - a.hhy * t1;
-                R vv = Wx(2, gj + 2, gi + 2) - a.hhy * t2;
-                R pp = Wx(3, gj + 2, gi + 2) - a.hhy * t3;
-                Rr.rho = rr; Rr.u = vv; Rr.v = -uu; Rr.p = pp;
-                Rr.drho = t0; Rr.du = t2; Rr.dv = -t1; Rr.dp = t3;
-                Rr.trho = -s0; Rr.tu = -s2; Rr.tv = s1; Rr.tp = -s3;
-            }
+            return !(j > m || i >= n);
         }
-        R p_start = R(-1);
-        if (LEARNED)
-            p_start = learned_guess_any<R>(L, Rr, active, a.G, Mlp);
-        if (!active)
-            continue;
+        const int g = f - NFX;
+        const int gj = g / (TI + 1), gi = g - gj * (TI + 1);
+        lj = gj; li = gi;
+        j = J0 + gj; i = I0 + gi;
+        // lower cell (i-1): slopes at (gj+1, gi), values at (gj+2, gi+1); rotated to the +y normal frame:
+        // normal velocity v, tangential -u; normal derivatives are the y-slopes, tangential the negated x-slopes
+        {
+            R t0 = Sx(4, gj + 1, gi), t1 = Sx(5, gj + 1, gi), t2 = Sx(6, gj + 1, gi), t3 = Sx(7, gj + 1, gi);
+            R s0 = Sx(0, gj + 1, gi), s1 = Sx(1, gj + 1, gi), s2 = Sx(2, gj + 1, gi), s3 = Sx(3, gj + 1, gi);
+            R rr = Wx(0, gj + 2, gi + 1) + a.hhy * t0;
+            R uu = Wx(1, gj + 2, gi + 1) + a.hhy * t1;
+            R vv = Wx(2, gj + 2, gi + 1) + a.hhy * t2;
+            R pp = Wx(3, gj + 2, gi + 1) + a.hhy * t3;
+            L.rho = rr; L.u = vv; L.v = -uu; L.p = pp;
+            L.drho = t0; L.du = t2; L.dv = -t1; L.dp = t3;
+            L.trho = -s0; L.tu = -s2; L.tv = s1; L.tp = -s3;
+        }
+        {
+            R t0 = Sx(4, gj + 1, gi + 1), t1 = Sx(5, gj + 1, gi + 1), t2 = Sx(6, gj + 1, gi + 1), t3 = Sx(7, gj + 1, gi + 1);
+            R s0 = Sx(0, gj + 1, gi + 1), s1 = Sx(1, gj + 1, gi + 1), s2 = Sx(2, gj + 1, gi + 1), s3 = Sx(3, gj + 1, gi + 1);
+            R rr = Wx(0, gj + 2, gi + 2) - a.hhy * t0;
+            R uu = Wx(1, gj + 2, gi + 2) - a.hhy * t1;
+            R vv = Wx(2, gj + 2, gi + 2) - a.hhy * t2;
+            R pp = Wx(3, gj + 2, gi + 2) - a.hhy * t3;
+            Rr.rho = rr; Rr.u = vv; Rr.v = -uu; Rr.p = pp;
+            Rr.drho = t0; Rr.du = t2; Rr.dv = -t1; Rr.dp = t3;
+            Rr.trho = -s0; Rr.tu = -s2; Rr.tv = s1; Rr.tp = -s3;
+        }
+        return !(j >= m || i > n);
+    };
+    // solve face f and store its flux and time derivative
+    auto solve_store = [&](auto known, int f, const Side<R>& L, const Side<R>& Rr, int lj, int li, int j, int i,
+                           R p_start) {
+        const bool ydir = f >= NFX;
         FaceOut<R> o;
-        int it;
-        int fbk;
-        const int code = solve_face<R>(L, Rr, a, o, it, fbk, ydir, p_start);
+        int it, fbk;
+        const int code = solve_face<R, decltype(known)::value>(L, Rr, a, o, it, fbk, ydir, p_start);
         if (it >= 0) {
             my_newton++;
             my_iters += it;
@@ -467,6 +515,60 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
                 FYx(4 + k, lj, li) = o.I[k];
             }
         }
+    };
+    __shared__ int s_qn;
+    if (tid == 0)
+        s_qn = 0;
+    __syncthreads();
+    // pass A: warp-uniform rounds so the queue appends are warp-aggregated
+    for (int fb = tid - lane; fb < NF; fb += NT) {
+        const int f = fb + lane;
+        Side<R> L, Rr;
+        int lj = 0, li = 0, j = 0, i = 0;
+        const bool active = f < NF && sides(f, L, Rr, lj, li, j, i);
+        const bool uni = active && face_uniform<R>(L, Rr, a.G);
+        const bool need = active && !uni;
+        const unsigned want = __ballot_sync(0xffffffffu, need);
+        if (want) {
+            int base = 0;
+            if (lane == 0)
+                base = atomicAdd(&s_qn, __popc(want));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (need)
+                Q[base + __popc(want & ((1u << lane) - 1u))] = (unsigned short)f;
+        }
+        if (uni)
+            solve_store(std::integral_constant<int, 1>(), f, L, Rr, lj, li, j, i, R(-1));
+    }
+    __syncthreads();
+    // pass B: the queued faces, 32 per warp.  The learned form first runs the
+    // network over the whole queue (warp-collective, tensor cores) and keeps
+    // each face's starting pressure in P, so the network and the exact solver
+    // never hold their registers at the same time.
+    const int qn = s_qn;
+    if constexpr (LEARNED) {
+        for (int qb = tid - lane; qb < qn; qb += NT) {
+            const int q = qb + lane;
+            const bool act = q < qn;
+            Side<R> L, Rr;
+            int lj = 0, li = 0, j = 0, i = 0;
+            sides(act ? (int)Q[q] : 0, L, Rr, lj, li, j, i);
+            const R g = learned_guess_any<R>(L, Rr, act, a.G, Mlp);
+            if (act)
+                P[q] = (float)g;
+        }
+        __syncthreads();
+    }
+    for (int qb = tid - lane; qb < qn; qb += NT) {
+        const int q = qb + lane;
+        if (q >= qn)
+            break;
+        const int f = (int)Q[q];
+        Side<R> L, Rr;
+        int lj = 0, li = 0, j = 0, i = 0;
+        sides(f, L, Rr, lj, li, j, i);
+        const R p_start = LEARNED ? (R)P[q] : R(-1);
+        solve_store(std::integral_constant<int, 2>(), f, L, Rr, lj, li, j, i, p_start);
     }
     if (a.stats) {
         // warp-aggregated statistics
@@ -494,7 +596,11 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
             continue;
         const size_t o = (size_t)j * a.ld + i;
         R rho = Wx(0, cj + 2, ci + 2), uu = Wx(1, cj + 2, ci + 2), vv = Wx(2, cj + 2, ci + 2);
-        R E = a.src_w[4 * a.plane + o];
+        R E;
+        if constexpr (STAGED)
+            E = Wx(4, cj + 2, ci + 2);
+        else
+            E = a.src_w[4 * a.plane + o];
         R mom_x = rho * uu - a.nu * (FXx(1, cj + 1, ci) - FXx(1, cj, ci)) - a.mu * (FYx(1, cj, ci + 1) - FYx(1, cj, ci));
         R mom_y = rho * vv - a.nu * (FXx(2, cj + 1, ci) - FXx(2, cj, ci)) - a.mu * (FYx(2, cj, ci + 1) - FYx(2, cj, ci));
         R ene = rho * E - a.nu * (FXx(3, cj + 1, ci) - FXx(3, cj, ci)) - a.mu * (FYx(3, cj, ci + 1) - FYx(3, cj, ci));
@@ -523,6 +629,21 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
 #undef FYx
 }
 
+// The gathered tile with its shared-memory carve-up (W | S | FX | FY).
+template <typename R, int TJ, int TI, int NT, bool LEARNED>
+__device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0, const int J0, unsigned char* smem_raw,
+                                             const MlpShared& Mlp)
+{
+    using SM = UnsplitSmem<R, TJ, TI>;
+    R* W = reinterpret_cast<R*>(smem_raw);
+    R* S = W + SM::nW;
+    R* FX = S + SM::nS;
+    R* FY = FX + SM::nFX;
+    unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + SM::bytes_f);
+    float* P = LEARNED ? reinterpret_cast<float*>(smem_raw + SM::p_off) : nullptr;
+    tile_body<R, TJ, TI, NT, LEARNED, false>(a, I0, J0, W, nullptr, S, FX, FY, Q, P, Mlp);
+}
+
 template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
 __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
 {
@@ -530,10 +651,102 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
     if (halt_prologue(a.ctl, a.seq))
         return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + (SM::bytes + 15) / 16 * 16);
+    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + SM::mlp_off);
     if (LEARNED)
         mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
     unsplit_tile<R, TJ, TI, NT, LEARNED>(a, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
+}
+
+// ---------------------------------------------------------------------------
+// persistent TMA-staged unsplit step: one CTA per SM walks the tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ...; while tile k is computed, the
+// TMA unit copies tile k+1's values and previous slopes into the other stage,
+// so global-memory latency overlaps the face solves.
+//   shared memory: stage 0 | stage 1 | S | FY | face queue | [network] | 2 mbarriers
+// (the x-fluxes FX reuse the slope box of the current stage, dead after the
+// limiter phase).
+// ---------------------------------------------------------------------------
+template <typename R, int TJ, int TI, bool LEARNED>
+struct TmaSmem {
+    using SM = UnsplitSmem<R, TJ, TI>;
+    using SL = StageLayout<R, TJ, TI>;
+    static constexpr size_t s_off = 2 * SL::bytes;
+    static constexpr size_t fy_off = s_off + sizeof(R) * SM::nS;
+    static constexpr size_t q_off = fy_off + sizeof(R) * SM::nFY;
+    static constexpr size_t p_off = (q_off + 2 * (size_t)SM::nQ + 15) / 16 * 16;
+    static constexpr size_t mlp_off = p_off + (LEARNED ? 4 * (size_t)SM::nQ : 0);
+    static constexpr size_t bar_off = (mlp_off + (LEARNED ? sizeof(MlpShared) : 0) + 15) / 16 * 16;
+    static constexpr size_t bytes = bar_off + 16;
+    static_assert(sizeof(R) * SM::nFX <= SL::b_bytes, "the x-fluxes must fit in the slope box they reuse");
+    static_assert(SL::bytes % 128 == 0, "stages start on 128-byte boundaries");
+};
+
+constexpr unsigned long long TMA_WAIT_NS = 2000000000ull;  // 2 s
+
+template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
+__global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ StepArgs<R> a,
+                                                       const __grid_constant__ StepMaps maps)
+{
+    using SL = StageLayout<R, TJ, TI>;
+    using TS = TmaSmem<R, TJ, TI, LEARNED>;
+    if (halt_prologue(a.ctl, a.seq))
+        return;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    R* S = reinterpret_cast<R*>(smem_raw + TS::s_off);
+    R* FY = reinterpret_cast<R*>(smem_raw + TS::fy_off);
+    unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + TS::q_off);
+    float* P = LEARNED ? reinterpret_cast<float*>(smem_raw + TS::p_off) : nullptr;
+    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + TS::mlp_off);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + TS::bar_off);
+    const int nti = (a.n + TI - 1) / TI;
+    const int ntiles = nti * ((a.m + TJ - 1) / TJ);
+    constexpr uint32_t STAGE_TX = (uint32_t)(SL::a_bytes + SL::b_bytes);
+    if (threadIdx.x == 0) {
+        tma_prefetch_desc(&maps.vals);
+        tma_prefetch_desc(&maps.slopes);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    if (LEARNED)
+        mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
+    __syncthreads();
+    // one thread: announce the stage's bytes and start its two box copies
+    auto issue = [&](int t, int stg) {
+        unsigned char* dst = smem_raw + stg * SL::bytes;
+        const int I0 = (t % nti) * TI, J0 = (t / nti) * TJ;
+        mbar_arrive_expect_tx(&bar[stg], STAGE_TX);
+        tma_load_3d(dst + SL::a_off, &maps.vals, I0 - SL::X, J0 - 2, 0, &bar[stg]);
+        tma_load_3d(dst + SL::b_off, &maps.slopes, I0 - SL::X, J0 - 1, 0, &bar[stg]);
+    };
+    int t = blockIdx.x, k = 0;
+    if (threadIdx.x == 0 && t < ntiles)
+        issue(t, 0);
+    bool failed = false;
+    for (; t < ntiles; ++k, t += gridDim.x) {
+        const int stg = k & 1;
+        if (threadIdx.x == 0 && t + (int)gridDim.x < ntiles) {
+            // the other stage was last read and written by tile k-1, which ended with a block barrier
+            fence_proxy_async_smem();
+            issue(t + gridDim.x, stg ^ 1);
+        }
+        const bool ok = mbar_wait_bounded(&bar[stg], (uint32_t)(k >> 1) & 1u, TMA_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        unsigned char* cur = smem_raw + stg * SL::bytes;
+        R* W = reinterpret_cast<R*>(cur + SL::a_off);
+        R* B = reinterpret_cast<R*>(cur + SL::b_off);
+        tile_body<R, TJ, TI, NT, LEARNED, true>(a, (t % nti) * TI, (t / nti) * TJ, W, B, S, B, FY, Q, P, Mlp);
+    }
+    if (failed && threadIdx.x == 0) {
+        // let the copies still in flight land (bounded) before the CTA exits, then report
+        mbar_wait_bounded(&bar[k & 1], (uint32_t)(k >> 1) & 1u, TMA_WAIT_NS);
+        if (t + (int)gridDim.x < ntiles)
+            mbar_wait_bounded(&bar[(k + 1) & 1], (uint32_t)((k + 1) >> 1) & 1u, TMA_WAIT_NS);
+        atomicExch(&a.ctl->wait_err, 1u);
+    }
 }
 
 // ---------------------------------------------------------------------------
