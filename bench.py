@@ -16,8 +16,9 @@ e2e         the same form through the reference's scheme call
 forms       plain FP32 and the FP64 parity form on the same grid and steps,
             relative L1 of every FP32 result against the FP64 result, FP64
             conservation integrals, Newton statistics.
-roofline    HBM roofline of the step kernel: 104 algorithmic bytes per
-            FP32 cell-update (13 planes read, 13 written, 4 B each).
+roofline    HBM roofline of the step kernel: 96 algorithmic bytes per FP32
+            cell-update (the carried state, 4 primitives + 8 limiter slopes,
+            read once and written once; 192 B in FP64).
 batch       512 independent four-quadrant problems, N x N with N uniform in
             {64, 96, ..., 512}, 300 steps, one persistent kernel under a CUDA
             graph with the autotuned tile shape and schedule.
@@ -44,8 +45,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "2D GRP cell-updates/s at 4096^2"
 UNIT = "cell-updates/s"
-BYTES_PER_CELL_F32 = 104.0   # 13 planes read + 13 written, 4 B
-BYTES_PER_CELL_F64 = 208.0
+BYTES_PER_CELL_F32 = 96.0    # 4 primitives + 8 slopes, read once and written once, 4 B
+BYTES_PER_CELL_F64 = 192.0
 
 
 def peaks():

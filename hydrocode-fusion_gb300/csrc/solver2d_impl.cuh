@@ -50,7 +50,7 @@ StepVariant<R> step_variant()
 template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false>
 StepVariant<R> tma_variant()
 {
-    return StepVariant<R>{TJ, TI, NT, MINB, TmaSmem<R, TJ, TI, LEARNED>::bytes,
+    return StepVariant<R>{TJ, TI, NT, MINB, TmaSmem<R, TJ, TI, LEARNED>::launch_bytes,
                           (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED>, 1, 0, {}};
 }
 
@@ -707,7 +707,8 @@ public:
         cudaEventElapsedTime(&ms, ev0, ev1);
         (void)wbuf_at_seq0;
         if (hc.wait_err) {
-            set_error("a bounded TMA wait in the step kernel gave up; the run is invalid");
+            set_error(hc.wait_err == 2 ? "the step kernel's TMA descriptor check failed; the run is invalid"
+                                       : "a bounded TMA wait in the step kernel gave up; the run is invalid");
             return -1;
         }
 

@@ -677,6 +677,9 @@ struct TmaSmem {
     static constexpr size_t mlp_off = p_off + (LEARNED ? 4 * (size_t)SM::nQ : 0);
     static constexpr size_t bar_off = (mlp_off + (LEARNED ? sizeof(MlpShared) : 0) + 15) / 16 * 16;
     static constexpr size_t bytes = bar_off + 16;
+    // the dynamic shared memory follows the static variables, so its start is
+    // only 16-byte aligned: 128 bytes of slack let the kernel align it itself
+    static constexpr size_t launch_bytes = bytes + 128;
     static_assert(sizeof(R) * SM::nFX <= SL::b_bytes, "the x-fluxes must fit in the slope box they reuse");
     static_assert(SL::bytes % 128 == 0, "stages start on 128-byte boundaries");
 };
@@ -691,7 +694,16 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
     using TS = TmaSmem<R, TJ, TI, LEARNED>;
     if (halt_prologue(a.ctl, a.seq))
         return;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_dyn[];
+    // tensor copies write to 128-byte aligned shared addresses only
+    unsigned char* smem_raw = smem_dyn + ((128u - (smem_addr(smem_dyn) & 127u)) & 127u);
+    if ((smem_addr(smem_raw) & 127u) != 0u || (reinterpret_cast<uintptr_t>(&maps.vals) & 63u) != 0u ||
+        (reinterpret_cast<uintptr_t>(&maps.slopes) & 63u) != 0u) {
+        // a misaligned stage or descriptor is never handed to the TMA unit
+        if (threadIdx.x == 0)
+            atomicExch(&a.ctl->wait_err, 2u);
+        return;
+    }
     R* S = reinterpret_cast<R*>(smem_raw + TS::s_off);
     R* FY = reinterpret_cast<R*>(smem_raw + TS::fy_off);
     unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + TS::q_off);
