@@ -200,4 +200,14 @@ __device__ __forceinline__ float warp_mlp(const float x[6], const MlpShared& S)
     return mine;
 }
 
+// The same forward pass out of line, for the step kernels: its fragment
+// registers then do not add to the register pressure of the whole tile code
+// (the network runs on a small fraction of the faces).  All 32 lanes call it.
+static __device__ __noinline__ float warp_mlp_outline(float x0, float x1, float x2, float x3, float x4, float x5,
+                                                      const MlpShared* S)
+{
+    const float x[6] = {x0, x1, x2, x3, x4, x5};
+    return warp_mlp(x, *S);
+}
+
 }  // namespace hydro

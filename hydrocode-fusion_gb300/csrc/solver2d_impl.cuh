@@ -374,7 +374,15 @@ public:
         if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y), "smem attr"))
             return -1;
-        if (const char* e = getenv("HYDRO_STEP_VARIANT")) {
+        // variant override for profiling: HYDRO_STEP_VARIANT_FP64 / _FP32 / _FP32_LEARNED,
+        // else HYDRO_STEP_VARIANT for every form
+        const char* fenv = form == HYDRO_FORM_FP64 ? "HYDRO_STEP_VARIANT_FP64"
+                           : form == HYDRO_FORM_FP32 ? "HYDRO_STEP_VARIANT_FP32"
+                                                     : "HYDRO_STEP_VARIANT_FP32_LEARNED";
+        const char* e = getenv(fenv);
+        if (!e)
+            e = getenv("HYDRO_STEP_VARIANT");
+        if (e) {
             int v = atoi(e);
             if (v >= 0 && v < (int)variants.size())
                 variant = v;

@@ -252,7 +252,7 @@ __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<
 #pragma unroll
             for (int k = 0; k < 6; ++k)
                 x[k] = 0.f;
-        const float y = warp_mlp(x, M);
+        const float y = warp_mlp_outline(x[0], x[1], x[2], x[3], x[4], x[5], &M);
         const bool vac = (Rr.u - L.u) >= 0.9f * 2.f * (cL + cR) / G.gm1;
         const float p = pbar * __expf(y);
         if (need && !vac && p > 0.f && p < INFINITY)
