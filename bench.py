@@ -58,13 +58,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_per_cell(kernel_key):
-    """DRAM bytes per cell-update of a kernel from the committed ncu summary."""
+def traffic_per_cell(form_key):
+    """DRAM bytes per cell-update of a form's step kernel from the committed
+    ncu summary, and the kernel configuration it was captured on."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return float(json.load(f)[kernel_key]["dram_bytes_per_cell"])
+            d = json.load(f)[form_key]
+        return float(d["dram_bytes_per_cell"]), d["kernel"]
     except Exception:
-        return None
+        return None, None
 
 
 class ClockSampler:
@@ -385,10 +387,12 @@ def main():
     kv = head["kernel_variant"]
     kname = "%s<float,%dx%d,%d,learned>" % ("k_step_tma" if kv.get("tma") else "k_step_unsplit", kv["tile_x"],
                                              kv["tile_y"], kv["threads"])
-    tpc = traffic_per_cell(kname)
+    tpc, tkern = traffic_per_cell("fp32_learned")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": tpc * m * n if tpc else None, "peak_source": peak_kind,
-            "kernel": kname + " (one launch per step)", "algorithmic_bytes_per_launch": BYTES_PER_CELL_F32 * m * n}
+            "kernel": kname + " (one launch per step)", "algorithmic_bytes_per_launch": BYTES_PER_CELL_F32 * m * n,
+            "traffic_source": f"ncu capture of {tkern} at 2048^2, scaled by cells (profiles/traffic.json)"
+            if tpc else None}
 
     forms = {
         "fp32_learned": summary(head, "f32") | {"l1_vs_fp64": accuracy(head)},

@@ -105,6 +105,30 @@ struct Gas {
     double g64, eps64;  // FP64 copies for the FP32 form's FP64 Newton fallback
 };
 
+// The constants of a Gas, derived in FP64 (host for the kernels' arguments;
+// device for the FP32 form's FP64 retry of a face).
+template <typename R>
+__host__ __device__ inline void gas_fill(Gas<R>& G, double g, double eps)
+{
+    double zeta = (g - 1.0) / (g + 1.0);
+    G.g = (R)g;
+    G.gm1 = (R)(g - 1.0);
+    G.zeta = (R)zeta;
+    G.mu = (R)((g - 1.0) / (2.0 * g));
+    G.nu = (R)((g + 1.0) / (2.0 * g));
+    G.g_g1 = (R)(g / (g - 1.0));
+    G.inv_g = (R)(1.0 / g);
+    G.cexp = (R)(0.5 * (g - 1.0) / g);
+    G.sexp = (R)(2.0 * g / (g - 1.0));
+    G.e1 = (R)(0.5 / zeta);
+    G.e2 = (R)((1.0 + zeta) / zeta);
+    G.opz = (R)(1.0 + zeta);
+    G.op2z = (R)(1.0 + 2.0 * zeta);
+    G.eps = (R)eps;
+    G.g64 = g;
+    G.eps64 = eps;
+}
+
 // Velocity on the 1-wave curve through (uL,pL) at pressure pp (shock for pp > pL,
 // rarefaction otherwise): riemann_solver_exact_Ben.c:50-62.
 template <typename R>

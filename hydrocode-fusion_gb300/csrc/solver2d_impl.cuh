@@ -181,23 +181,7 @@ __global__ void k_cfl_min(const R* __restrict__ w, size_t plane, int m, int n, i
 template <typename R>
 void fill_gas_params(Gas<R>& G, double g, double eps)
 {
-    double zeta = (g - 1.0) / (g + 1.0);
-    G.g = (R)g;
-    G.gm1 = (R)(g - 1.0);
-    G.zeta = (R)zeta;
-    G.mu = (R)((g - 1.0) / (2.0 * g));
-    G.nu = (R)((g + 1.0) / (2.0 * g));
-    G.g_g1 = (R)(g / (g - 1.0));
-    G.inv_g = (R)(1.0 / g);
-    G.cexp = (R)(0.5 * (g - 1.0) / g);
-    G.sexp = (R)(2.0 * g / (g - 1.0));
-    G.e1 = (R)(0.5 / zeta);
-    G.e2 = (R)((1.0 + zeta) / zeta);
-    G.opz = (R)(1.0 + zeta);
-    G.op2z = (R)(1.0 + 2.0 * zeta);
-    G.eps = (R)eps;
-    G.g64 = g;
-    G.eps64 = eps;
+    gas_fill(G, g, eps);
 }
 
 // Conservation sums in FP64: mass, x/y momentum and total energy,

@@ -212,6 +212,39 @@ __device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigne
         atomicMax(&ctl->key[slot][dir], ((serial + 1ull) << 2) | (unsigned long long)code);
 }
 
+// FP32 form: a face whose GRP star state fails the positivity / finiteness
+// check in FP32 arithmetic is solved again in FP64 from the same
+// (FP32-reconstructed) sides, and the FP64 result is kept when it passes.
+// Out of line: it runs on a handful of faces per run.
+static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, const Side<float>& Rr, double g,
+                                                         double eps, double tau, bool ydir, FaceOut<float>& o)
+{
+    Gas<double> G;
+    gas_fill(G, g, eps);
+    Side<double> Ld, Rd;
+    Ld.rho = L.rho; Ld.u = L.u; Ld.v = L.v; Ld.p = L.p;
+    Ld.drho = L.drho; Ld.du = L.du; Ld.dv = L.dv; Ld.dp = L.dp;
+    Ld.trho = L.trho; Ld.tu = L.tu; Ld.tv = L.tv; Ld.tp = L.tp;
+    Rd.rho = Rr.rho; Rd.u = Rr.u; Rd.v = Rr.v; Rd.p = Rr.p;
+    Rd.drho = Rr.drho; Rd.du = Rr.du; Rd.dv = Rr.dv; Rd.dp = Rr.dp;
+    Rd.trho = Rr.trho; Rd.tu = Rr.tu; Rd.tv = Rr.tv; Rd.tp = Rr.tp;
+    Star<double> S;
+    StarInfo st;
+    st.fallback = 0;
+    q1d_star<double, 0>(Ld, Rd, G, S, st, -1.0);
+    double D[4], U[4];
+    q1d_derivs(Ld, Rd, G, S, D, U);
+    const int bad = star_dire_check2(U, D, eps);
+    FaceOut<double> od;
+    face_flux<double>(D, U, tau, 0.5 * tau, G, od, ydir);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        o.F[k] = (float)od.F[k];
+        o.I[k] = (float)od.I[k];
+    }
+    return bad;
+}
+
 // Solve one face given its two sides in the face's normal frame (KNOWN as in
 // q1d_star: whether the uniform-pair decision has already been made).
 template <typename R, int KNOWN = 0>
@@ -225,11 +258,18 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
     q1d_star<R, KNOWN>(L, Rr, a.G, S, st, p_start);
     R D[4], U[4];
     q1d_derivs(L, Rr, a.G, S, D, U);
-    if (star_dire_check2(U, D, a.G.eps))
-        code = 2;
-    face_flux<R>(D, U, a.tau, a.htau, a.G, o, ydir);
     iters = st.iters;
     fallback = st.fallback;
+    if (star_dire_check2(U, D, a.G.eps)) {
+        if constexpr (sizeof(R) == 4) {
+            if (solve_face_fp64_retry(L, Rr, a.G.g64, a.G.eps64, (double)a.tau, ydir, o) == 0) {
+                fallback = 1;
+                return code;
+            }
+        }
+        code = 2;
+    }
+    face_flux<R>(D, U, a.tau, a.htau, a.G, o, ydir);
     return code;
 }
 
