@@ -115,6 +115,22 @@ struct MlpShared {
     float b1[MLP_H], b2[MLP_H], b3;
 };
 
+// The shared-memory image built once in global memory (for kernels that read
+// the network through L1 instead of staging it in shared memory).
+static __global__ void k_mlp_image(const uint32_t* __restrict__ frag, const float* __restrict__ prm,
+                                   MlpShared* __restrict__ img)
+{
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int q = tid; q < MLP_NFRAG; q += gridDim.x * blockDim.x)
+        img->frag[q] = frag[q];
+    if (tid < MLP_H) {
+        img->b1[tid] = prm[MLP_B1 + tid];
+        img->b2[tid] = prm[MLP_B2 + tid];
+    }
+    if (tid == 0)
+        img->b3 = prm[MLP_B3];
+}
+
 __device__ __forceinline__ void mlp_load_shared(MlpShared& S, const uint32_t* __restrict__ frag,
                                                 const float* __restrict__ prm, int tid, int nthreads)
 {

@@ -27,8 +27,9 @@ namespace hydro {
 // Compiled configurations of the unsplit step kernel (tile TJ x TI cells,
 // NT threads, at least MINB resident CTAs per SM requested from ptxas).  The
 // autotuner (Solver2D::autotune) times them on the actual problem.
-// tma = 1: the persistent TMA-staged kernel (k_step_tma), launched with
-// occ CTAs per SM; tma = 0: one CTA per tile (k_step_unsplit).
+// tma = 1 or 2: the persistent TMA-staged kernel (k_step_tma) with that many
+// shared-memory stages, launched with occ CTAs per SM; tma = 0: one CTA per
+// tile (k_step_unsplit).
 template <typename R>
 struct StepVariant {
     int TJ, TI, NT, MINB;
@@ -47,11 +48,11 @@ StepVariant<R> step_variant()
                           (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED>, 0, 0, {}};
 }
 
-template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false>
+template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int STAGES = 2>
 StepVariant<R> tma_variant()
 {
-    return StepVariant<R>{TJ, TI, NT, MINB, TmaSmem<R, TJ, TI, LEARNED>::launch_bytes,
-                          (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED>, 1, 0, {}};
+    return StepVariant<R>{TJ, TI, NT, MINB, TmaSmem<R, TJ, TI, LEARNED, STAGES>::launch_bytes,
+                          (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED, STAGES>, STAGES, 0, {}};
 }
 
 template <typename R> struct Variants;
@@ -71,13 +72,15 @@ template <> struct Variants<float> {
             return {step_variant<float, 32, 32, 512, 1, true>(), step_variant<float, 16, 32, 512, 1, true>(),
                     step_variant<float, 16, 32, 512, 2, true>(), step_variant<float, 16, 16, 256, 2, true>(),
                     step_variant<float, 16, 16, 256, 3, true>(), tma_variant<float, 32, 32, 512, 1, true>(),
-                    tma_variant<float, 16, 32, 512, 1, true>(), tma_variant<float, 16, 16, 256, 3, true>()};
+                    tma_variant<float, 16, 32, 512, 1, true>(), tma_variant<float, 16, 16, 256, 3, true>(),
+                    tma_variant<float, 16, 32, 256, 2, true, 1>()};
         return {step_variant<float, 16, 32, 512, 1>(), step_variant<float, 16, 16, 256, 2>(),
                 step_variant<float, 16, 16, 256, 3>(), step_variant<float, 16, 16, 256, 4>(),
                 step_variant<float, 8, 32, 256, 3>(),  step_variant<float, 32, 32, 512, 1>(),
                 step_variant<float, 16, 32, 512, 2>(), tma_variant<float, 32, 32, 512, 1>(),
                 tma_variant<float, 16, 32, 512, 1>(), tma_variant<float, 16, 16, 256, 3>(),
-                tma_variant<float, 8, 32, 256, 3>()};
+                tma_variant<float, 8, 32, 256, 3>(), tma_variant<float, 16, 32, 256, 2, false, 1>(),
+                tma_variant<float, 32, 32, 512, 1, false, 1>()};
     }
     static constexpr int SJ = 16, SI = 32, SNT = 256;
 };
@@ -311,7 +314,8 @@ public:
         variants = TS::all(form == HYDRO_FORM_FP32_LEARNED);
         if (form == HYDRO_FORM_FP32_LEARNED) {
             if (!cuda_ok(cudaMalloc(&mlp_frag, sizeof(uint32_t) * MLP_NFRAG), "network") ||
-                !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network"))
+                !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network") ||
+                !cuda_ok(cudaMalloc(&mlp_img, sizeof(MlpShared)), "network"))
                 return -1;
         }
         int smem_optin = 0;
@@ -377,6 +381,7 @@ public:
 
     uint32_t* mlp_frag = nullptr;
     float* mlp_prm = nullptr;
+    MlpShared* mlp_img = nullptr;
     bool mlp_set = false;
 
     int set_mlp(const float* params) override
@@ -389,7 +394,8 @@ public:
                      "network upload"))
             return -1;
         k_mlp_pack<<<(8 * 32 + 4 * 8 * 32 + 4 * 32 + 127) / 128, 128, 0, stream>>>(mlp_prm, mlp_frag);
-        count_launch();
+        k_mlp_image<<<(MLP_NFRAG + 255) / 256, 256, 0, stream>>>(mlp_frag, mlp_prm, mlp_img);
+        count_launch(2);
         mlp_set = true;
         return cuda_ok(cudaStreamSynchronize(stream), "network pack") ? 0 : -1;
     }
@@ -399,6 +405,7 @@ public:
         if (stream) cudaStreamSynchronize(stream);
         cudaFree(mlp_frag);
         cudaFree(mlp_prm);
+        cudaFree(mlp_img);
         cudaFree(mem);
         cudaFree(ghost0);
         cudaFree(ctl);
@@ -613,6 +620,7 @@ public:
             }
             a.mlp_frag = mlp_frag;
             a.mlp_prm = mlp_prm;
+            a.mlp_img = mlp_img;
         }
 
         using TS = Variants<R>;

@@ -77,6 +77,7 @@ struct StepArgs {
     int stats;             // count Newton faces / iterations
     const uint32_t* mlp_frag;  // learned form: packed BF16 network
     const float* mlp_prm;      // learned form: FP32 parameters (biases)
+    const MlpShared* mlp_img;  // learned form: the same image in global memory (read through L1)
 };
 
 // ---------------------------------------------------------------------------
@@ -698,24 +699,28 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
 }
 
 // ---------------------------------------------------------------------------
-// persistent TMA-staged unsplit step: one CTA per SM walks the tiles
-// t = blockIdx.x, blockIdx.x + gridDim.x, ...; while tile k is computed, the
-// TMA unit copies tile k+1's values and previous slopes into the other stage,
-// so global-memory latency overlaps the face solves.
-//   shared memory: stage 0 | stage 1 | S | FY | face queue | [network] | 2 mbarriers
+// persistent TMA-staged unsplit step: resident CTAs walk the tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ...  With STAGES = 2, while tile k
+// is computed the TMA unit copies tile k+1's values and previous slopes into
+// the other stage, so global-memory latency overlaps the face solves within
+// the CTA; with STAGES = 1 the CTA waits for its own copy and the other CTAs
+// on the SM hide it (smaller shared memory, more CTAs per SM).
+//   shared memory: stage(s) | S | FY | face queue | [starting pressures] | 2 mbarriers
 // (the x-fluxes FX reuse the slope box of the current stage, dead after the
-// limiter phase).
+// limiter phase; the learned form reads its network from global memory).
 // ---------------------------------------------------------------------------
-template <typename R, int TJ, int TI, bool LEARNED>
+template <typename R, int TJ, int TI, bool LEARNED, int STAGES = 2>
 struct TmaSmem {
     using SM = UnsplitSmem<R, TJ, TI>;
     using SL = StageLayout<R, TJ, TI>;
-    static constexpr size_t s_off = 2 * SL::bytes;
+    static_assert(STAGES == 1 || STAGES == 2, "one or two stages");
+    static constexpr size_t s_off = STAGES * SL::bytes;
     static constexpr size_t fy_off = s_off + sizeof(R) * SM::nS;
     static constexpr size_t q_off = fy_off + sizeof(R) * SM::nFY;
     static constexpr size_t p_off = (q_off + 2 * (size_t)SM::nQ + 15) / 16 * 16;
     static constexpr size_t mlp_off = p_off + (LEARNED ? 4 * (size_t)SM::nQ : 0);
-    static constexpr size_t bar_off = (mlp_off + (LEARNED ? sizeof(MlpShared) : 0) + 15) / 16 * 16;
+    // the network stays in global memory here (a.mlp_img, cached in L1): shared memory is full
+    static constexpr size_t bar_off = (mlp_off + 15) / 16 * 16;
     static constexpr size_t bytes = bar_off + 16;
     // the dynamic shared memory follows the static variables, so its start is
     // only 16-byte aligned: 128 bytes of slack let the kernel align it itself
@@ -726,12 +731,12 @@ struct TmaSmem {
 
 constexpr unsigned long long TMA_WAIT_NS = 2000000000ull;  // 2 s
 
-template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
+template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false, int STAGES = 2>
 __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ StepArgs<R> a,
                                                        const __grid_constant__ StepMaps maps)
 {
     using SL = StageLayout<R, TJ, TI>;
-    using TS = TmaSmem<R, TJ, TI, LEARNED>;
+    using TS = TmaSmem<R, TJ, TI, LEARNED, STAGES>;
     if (halt_prologue(a.ctl, a.seq))
         return;
     extern __shared__ __align__(128) unsigned char smem_dyn[];
@@ -748,7 +753,7 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
     R* FY = reinterpret_cast<R*>(smem_raw + TS::fy_off);
     unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + TS::q_off);
     float* P = LEARNED ? reinterpret_cast<float*>(smem_raw + TS::p_off) : nullptr;
-    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + TS::mlp_off);
+    const MlpShared& Mlp = *(LEARNED ? a.mlp_img : reinterpret_cast<const MlpShared*>(smem_raw));
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + TS::bar_off);
     const int nti = (a.n + TI - 1) / TI;
     const int ntiles = nti * ((a.m + TJ - 1) / TJ);
@@ -760,8 +765,6 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
         mbar_init(&bar[1], 1);
         fence_mbar_init();
     }
-    if (LEARNED)
-        mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
     __syncthreads();
     // one thread: announce the stage's bytes and start its two box copies
     auto issue = [&](int t, int stg) {
@@ -772,17 +775,28 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
         tma_load_3d(dst + SL::b_off, &maps.slopes, I0 - SL::X, J0 - 1, 0, &bar[stg]);
     };
     int t = blockIdx.x, k = 0;
-    if (threadIdx.x == 0 && t < ntiles)
+    if (STAGES == 2 && threadIdx.x == 0 && t < ntiles)
         issue(t, 0);
     bool failed = false;
     for (; t < ntiles; ++k, t += gridDim.x) {
-        const int stg = k & 1;
-        if (threadIdx.x == 0 && t + (int)gridDim.x < ntiles) {
-            // the other stage was last read and written by tile k-1, which ended with a block barrier
-            fence_proxy_async_smem();
-            issue(t + gridDim.x, stg ^ 1);
+        // stage of tile k and the parity of its barrier's phase (the j-th use of
+        // a barrier completes phase j)
+        const int stg = STAGES == 2 ? (k & 1) : 0;
+        const uint32_t parity = STAGES == 2 ? (uint32_t)(k >> 1) & 1u : (uint32_t)k & 1u;
+        if (threadIdx.x == 0) {
+            if (STAGES == 2) {
+                if (t + (int)gridDim.x < ntiles) {
+                    // the other stage was last read and written by tile k-1, which ended with a block barrier
+                    fence_proxy_async_smem();
+                    issue(t + gridDim.x, stg ^ 1);
+                }
+            } else {
+                // the only stage was last used by tile k-1, which ended with a block barrier
+                fence_proxy_async_smem();
+                issue(t, 0);
+            }
         }
-        const bool ok = mbar_wait_bounded(&bar[stg], (uint32_t)(k >> 1) & 1u, TMA_WAIT_NS);
+        const bool ok = mbar_wait_bounded(&bar[stg], parity, TMA_WAIT_NS);
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
@@ -794,9 +808,13 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
     }
     if (failed && threadIdx.x == 0) {
         // let the copies still in flight land (bounded) before the CTA exits, then report
-        mbar_wait_bounded(&bar[k & 1], (uint32_t)(k >> 1) & 1u, TMA_WAIT_NS);
-        if (t + (int)gridDim.x < ntiles)
-            mbar_wait_bounded(&bar[(k + 1) & 1], (uint32_t)((k + 1) >> 1) & 1u, TMA_WAIT_NS);
+        if (STAGES == 2) {
+            mbar_wait_bounded(&bar[k & 1], (uint32_t)(k >> 1) & 1u, TMA_WAIT_NS);
+            if (t + (int)gridDim.x < ntiles)
+                mbar_wait_bounded(&bar[(k + 1) & 1], (uint32_t)((k + 1) >> 1) & 1u, TMA_WAIT_NS);
+        } else {
+            mbar_wait_bounded(&bar[0], (uint32_t)k & 1u, TMA_WAIT_NS);
+        }
         atomicExch(&a.ctl->wait_err, 1u);
     }
 }

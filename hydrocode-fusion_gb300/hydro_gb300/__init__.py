@@ -218,7 +218,7 @@ class Solver2D:
         shape = (ctypes.c_int * 5)()
         v = lib().hydro2d_get_variant(self._h, shape)
         return int(v), {"tile_x": shape[0], "tile_y": shape[1], "threads": shape[2], "min_ctas_per_sm": shape[3],
-                        "tma": bool(shape[4])}
+                        "tma": bool(shape[4]), "tma_stages": int(shape[4])}
 
     def autotune(self, cfg, steps=3):
         """Time every kernel variant on `steps` steps of the uploaded state (restored

@@ -118,7 +118,7 @@ int hydro1d_run(int m, double *rho, double *u, double *p, double *E, const doubl
                 hydro_run_info *info);
 /* Kernel variants of the unsplit step (tile shape / threads / occupancy).
  * hydro2d_get_variant fills shape[5] = {tile x, tile y, threads, min CTAs per SM,
- * 1 for the persistent TMA-staged kernel / 0 for one CTA per tile}. */
+ * shared-memory stages of the persistent TMA-staged kernel (1 or 2), 0 for one CTA per tile}. */
 int hydro2d_num_variants(hydro2d_t *h);
 int hydro2d_set_variant(hydro2d_t *h, int v);
 int hydro2d_get_variant(hydro2d_t *h, int *shape);
