@@ -31,8 +31,14 @@
 
 namespace hydro {
 
+// Step arguments of a problem come in BATCH_VERSIONS ready-made versions, so a
+// tile only copies them: (step & 1) * 3 + step % 3 for steps >= 2 (buffer
+// parity and error-key slot), and 6 for step 1 (first limiting: minmod2).
+constexpr int BATCH_VERSIONS = 7;
+__host__ __device__ inline int batch_version(int step) { return step == 1 ? 6 : (step & 1) * 3 + step % 3; }
+
 struct BatchDev {
-    const StepArgs<float>* args;  // [nprob][2]: index 2p + (step & 1)
+    const StepArgs<float>* args;  // [nprob][BATCH_VERSIONS]
     Ctl* ctl;                     // [nprob]
     const int* tile_prob;         // [ntiles] problem of each flat tile
     const int* tile_local;        // [ntiles] tile index within its problem (y-tiles fastest)
@@ -88,43 +94,42 @@ __device__ __forceinline__ bool grid_barrier(const BatchDev& B)
 
 // Loads the step arguments of flat tile t into shared memory and applies the
 // one-problem kernel's halting protocol (halt_prologue) per problem.  Returns
-// false (uniformly over the block) when the tile's problem has halted.
+// false (uniformly over the block) when the tile's problem has halted.  Every
+// thread makes the halting decision from the same control block (the keys it
+// reads were final at the previous step's barrier, so all agree), and the
+// block copies the arguments word by word: one barrier per tile.
 __device__ __forceinline__ bool batch_tile_args(const BatchDev& B, int t, int step, StepArgs<float>& sa, int& lt)
 {
-    __shared__ int s_ok;
     const int p = B.tile_prob[t];
     lt = B.tile_local[t];
-    if (threadIdx.x == 0) {
-        volatile Ctl* c = B.ctl + p;
-        int ok = c->halted_seq == 0;
-        if (ok && step > 1) {
-            const int ps = (step - 1) % 3;
-            const int d = halt_decision(c->key[ps][0], c->key[ps][1], c->upd_bad[ps]);
-            if (d) {
-                ok = 0;
-                if (lt == 0) {
-                    c->halt_kind = d;
-                    c->halted_seq = step - 1;
-                }
+    volatile Ctl* c = B.ctl + p;
+    bool ok = c->halted_seq == 0;
+    if (ok && step > 1) {
+        const int ps = (step - 1) % 3;
+        const int d = halt_decision(c->key[ps][0], c->key[ps][1], c->upd_bad[ps]);
+        if (d) {
+            ok = false;
+            if (lt == 0 && threadIdx.x == 0) {
+                c->halt_kind = d;
+                c->halted_seq = step - 1;
             }
         }
-        if (ok && lt == 0) {
+    }
+    if (ok) {
+        if (lt == 0 && threadIdx.x == 0) {
             const int ns = (step + 1) % 3;
             c->key[ns][0] = 0ull;
             c->key[ns][1] = 0ull;
             c->upd_bad[ns] = 0u;
         }
-        if (ok) {
-            sa = B.args[2 * p + (step & 1)];
-            sa.seq = step;
-            sa.find_x = sa.find_y = (step > 1);
-            sa.stats = B.stats;
-        }
-        s_ok = ok;
+        constexpr int WORDS = (int)(sizeof(StepArgs<float>) / 4);
+        static_assert(sizeof(StepArgs<float>) % 4 == 0, "word copy");
+        const int* src = reinterpret_cast<const int*>(B.args + (size_t)p * BATCH_VERSIONS + batch_version(step));
+        int* dst = reinterpret_cast<int*>(&sa);
+        for (int w = threadIdx.x; w < WORDS; w += blockDim.x)
+            dst[w] = src[w];
     }
     __syncthreads();
-    const bool ok = s_ok != 0;
-    __syncthreads();  // s_ok is rewritten for the next tile
     return ok;
 }
 
@@ -255,14 +260,14 @@ struct hydro_batch {
 };
 
 // Host side of one run: per-problem plans, step arguments and tile tables.
-static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps, const BatchShape& S, int schedule,
-                         int* ntiles)
+static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps, int stats, const BatchShape& S,
+                         int schedule, int* ntiles)
 {
     const int np = b->nprob;
     RunConfig rc = run_config_from(cfg, ncfg);
     rc.N = steps;
     rc.t_all = INFINITY;  // fixed step count
-    std::vector<StepArgs<float>> args(2 * (size_t)np);
+    std::vector<StepArgs<float>> args(BATCH_VERSIONS * (size_t)np);
     b->tau.assign(np, 0.0);
     for (int p = 0; p < np; ++p) {
         const int m = b->m[p], n = b->n[p], ld = b->ld[p];
@@ -296,9 +301,17 @@ static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps,
                 return -1;
             }
         b->tau[p] = r0.tau_face;
-        for (int par = 0; par < 2; ++par) {
-            StepArgs<float>& a = args[2 * p + par];
+        for (int ver = 0; ver < BATCH_VERSIONS; ++ver) {
+            // a representative step of this version (same parity, slot and first-step flag)
+            int step = 1;
+            while (batch_version(step) != ver)
+                ++step;
+            const int par = step & 1;
+            StepArgs<float>& a = args[(size_t)p * BATCH_VERSIONS + ver];
             memset(&a, 0, sizeof(a));
+            a.seq = step;
+            a.find_x = a.find_y = (step > 1);
+            a.stats = stats;
             a.m = m;
             a.n = n;
             a.ld = ld;
@@ -372,7 +385,8 @@ static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps,
     cudaMemcpyAsync(b->tables + nt, tlocal.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, b->stream);
     cudaMemcpyAsync(b->tables + 2 * (size_t)nt, order.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, b->stream);
     cudaMemcpyAsync(b->tables + 3 * (size_t)nt, ty.data(), sizeof(int) * np, cudaMemcpyHostToDevice, b->stream);
-    cudaMemcpyAsync(b->args, args.data(), sizeof(StepArgs<float>) * 2 * np, cudaMemcpyHostToDevice, b->stream);
+    cudaMemcpyAsync(b->args, args.data(), sizeof(StepArgs<float>) * BATCH_VERSIONS * np, cudaMemcpyHostToDevice,
+                    b->stream);
     *ntiles = nt;
     return cuda_ok(cudaStreamSynchronize(b->stream), "batch prepare") ? 0 : -1;
 }
@@ -452,7 +466,7 @@ int hydro_batch_create(hydro_batch** out, int nprob, const int* m, const int* n)
         !cuda_ok(cudaMemset(b->mem, 0, sizeof(float) * b->off[nprob]), "batch clear") ||
         !cuda_ok(cudaMalloc(&b->ghost, sizeof(float) * b->goff[nprob]), "batch boundary tables") ||
         !cuda_ok(cudaMalloc(&b->ctl, sizeof(Ctl) * nprob), "batch control blocks") ||
-        !cuda_ok(cudaMalloc(&b->args, sizeof(StepArgs<float>) * 2 * nprob), "batch step arguments") ||
+        !cuda_ok(cudaMalloc(&b->args, sizeof(StepArgs<float>) * BATCH_VERSIONS * nprob), "batch step arguments") ||
         !cuda_ok(cudaMalloc(&b->sync, sizeof(unsigned int) * 8), "batch barrier") ||
         !cuda_ok(cudaMalloc(&b->stage, sizeof(double) * 5 * maxmn), "batch staging") ||
         !cuda_ok(cudaMalloc(&b->red, sizeof(unsigned long long)), "batch reduction") ||
@@ -581,7 +595,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
     }
     const BatchShape& S = batch_shapes()[b->shape];
     int nt = 0;
-    if (batch_prepare(b, cfg, ncfg, steps, S, b->schedule, &nt))
+    if (batch_prepare(b, cfg, ncfg, steps, stats, S, b->schedule, &nt))
         return -1;
     BatchDev B;
     memset(&B, 0, sizeof(B));

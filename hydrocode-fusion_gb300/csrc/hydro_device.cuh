@@ -422,7 +422,8 @@ __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, co
         st.fallback = 0;
         return;
     }
-    q1d_star_exact(L, Rr, G, S, st, p_start);
+    if constexpr (KNOWN != 1)  // no out-of-line call (and its addressed arguments) on the uniform path
+        q1d_star_exact(L, Rr, G, S, st, p_start);
 }
 
 // Waves of the star state (linear_grp_solver_Edir_Q1D.c:110-133).
@@ -459,7 +460,8 @@ __device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& R
 
 // Time derivatives D and t-axis values U of the quasi-1D GRP given the star
 // state: linear_grp_solver_Edir_Q1D.c:139-545 with lambda = 0.
-template <typename R>
+// KNOWN as in q1d_star (1: S is the acoustic case, 2: it is not).
+template <typename R, int KNOWN = 0>
 __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
                                            R D[4], R U[4])
 {
@@ -474,7 +476,7 @@ __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, 
     const R zetaL = G.zeta, zetaR = G.zeta, gL = G.g, gR = G.g;
     R C = R(0);
 
-    if (S.acoustic) {  // acoustic case (:139-254); CRW branches are unreachable here
+    if (KNOWN != 2 && S.acoustic) {  // acoustic case (:139-254); CRW branches are unreachable here
         if (S.speed_L > R(0)) {
             U[0] = rho_L; U[1] = u_L; U[2] = v_L; U[3] = p_L;
             D[0] = -u_L * d_rho_L - v_L * t_rho_L - rho_L * (d_u_L + t_v_L);
@@ -522,7 +524,8 @@ __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, 
         D[3] = -U[1] * D_p - U[2] * T_p - U[0] * C * C * (D_u + T_v);
         return;
     }
-    q1d_derivs_exact(L, Rr, G, S, D, U);
+    if constexpr (KNOWN != 1)
+        q1d_derivs_exact(L, Rr, G, S, D, U);
 }
 
 // Non-acoustic case of the quasi-1D GRP (:256-547), out of line like q1d_star_exact.

@@ -215,8 +215,9 @@ __device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigne
 
 // FP32 form: a face whose GRP star state fails the positivity / finiteness
 // check in FP32 arithmetic is solved again in FP64 from the same
-// (FP32-reconstructed) sides, and the FP64 result is kept when it passes.
-// Out of line: it runs on a handful of faces per run.
+// (FP32-reconstructed) sides; returns the face's error code (0, 1 or 2) as
+// the FP64 solve sees it.  Out of line and called from a separate pass after
+// the face passes: it runs on a handful of faces per run.
 static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, const Side<float>& Rr, double g,
                                                          double eps, double tau, bool ydir, FaceOut<float>& o)
 {
@@ -235,7 +236,7 @@ static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, c
     q1d_star<double, 0>(Ld, Rd, G, S, st, -1.0);
     double D[4], U[4];
     q1d_derivs(Ld, Rd, G, S, D, U);
-    const int bad = star_dire_check2(U, D, eps);
+    const int bad = star_dire_check2(U, D, eps) ? 2 : (ifvar_bad(Ld, Rd, eps) ? 1 : 0);
     FaceOut<double> od;
     face_flux<double>(D, U, tau, 0.5 * tau, G, od, ydir);
 #pragma unroll
@@ -258,18 +259,11 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
     st.fallback = 0;
     q1d_star<R, KNOWN>(L, Rr, a.G, S, st, p_start);
     R D[4], U[4];
-    q1d_derivs(L, Rr, a.G, S, D, U);
+    q1d_derivs<R, KNOWN>(L, Rr, a.G, S, D, U);
     iters = st.iters;
     fallback = st.fallback;
-    if (star_dire_check2(U, D, a.G.eps)) {
-        if constexpr (sizeof(R) == 4) {
-            if (solve_face_fp64_retry(L, Rr, a.G.g64, a.G.eps64, (double)a.tau, ydir, o) == 0) {
-                fallback = 1;
-                return code;
-            }
-        }
+    if (star_dire_check2(U, D, a.G.eps))
         code = 2;
-    }
     face_flux<R>(D, U, a.tau, a.htau, a.G, o, ydir);
     return code;
 }
@@ -477,6 +471,11 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
     constexpr int NFX = (TJ + 1) * TI, NFY = TJ * (TI + 1), NF = NFX + NFY;
     int my_iters = 0, my_newton = 0, my_fb = 0;
     const int lane = tid & 31;
+    __shared__ int s_qn;
+    // FP32 faces whose star state failed its check, solved again in FP64 after the passes
+    constexpr int RETRY_MAX = 128;
+    __shared__ int s_nretry;
+    __shared__ unsigned short s_retry[RETRY_MAX];
     // sides of face f (x-faces first, then y-faces) in the face's normal frame;
     // false when the face lies outside the domain
     auto sides = [&](int f, Side<R>& L, Side<R>& Rr, int& lj, int& li, int& j, int& i) -> bool {
@@ -535,11 +534,19 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
         const bool ydir = f >= NFX;
         FaceOut<R> o;
         int it, fbk;
-        const int code = solve_face<R, decltype(known)::value>(L, Rr, a, o, it, fbk, ydir, p_start);
+        int code = solve_face<R, decltype(known)::value>(L, Rr, a, o, it, fbk, ydir, p_start);
         if (it >= 0) {
             my_newton++;
             my_iters += it;
             my_fb += fbk;
+        }
+        if (sizeof(R) == 4 && code == 2) {
+            // FP32 star state failed its check: solve this face again in FP64 after the passes
+            const int r = atomicAdd(&s_nretry, 1);
+            if (r < RETRY_MAX) {
+                s_retry[r] = (unsigned short)f;
+                code = 0;  // reported by the retry
+            }
         }
         if (!ydir) {
             report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
@@ -557,9 +564,10 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
             }
         }
     };
-    __shared__ int s_qn;
-    if (tid == 0)
+    if (tid == 0) {
         s_qn = 0;
+        s_nretry = 0;
+    }
     __syncthreads();
     // pass A: warp-uniform rounds so the queue appends are warp-aggregated
     for (int fb = tid - lane; fb < NF; fb += NT) {
@@ -627,6 +635,36 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
         }
     }
     __syncthreads();
+    if constexpr (sizeof(R) == 4) {
+        const int nr = s_nretry < RETRY_MAX ? s_nretry : RETRY_MAX;
+        if (nr > 0) {
+            for (int r = tid; r < nr; r += NT) {
+                const int f = (int)s_retry[r];
+                Side<R> L, Rr;
+                int lj = 0, li = 0, j = 0, i = 0;
+                sides(f, L, Rr, lj, li, j, i);
+                FaceOut<R> o;
+                const bool ydir = f >= NFX;
+                const int code = solve_face_fp64_retry(L, Rr, a.G.g64, a.G.eps64, (double)a.tau, ydir, o);
+                if (!ydir) {
+                    report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        FXx(k, lj, li) = o.F[k];
+                        FXx(4 + k, lj, li) = o.I[k];
+                    }
+                } else {
+                    report_face(a.ctl, slot, 1, (unsigned long long)j * (n + 1) + i, code);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        FYx(k, lj, li) = o.F[k];
+                        FYx(4 + k, lj, li) = o.I[k];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
 
     // 4. conservative update and new slopes
     unsigned bad = 0;
