@@ -73,14 +73,16 @@ template <> struct Variants<float> {
                     step_variant<float, 16, 32, 512, 2, true>(), step_variant<float, 16, 16, 256, 2, true>(),
                     step_variant<float, 16, 16, 256, 3, true>(), tma_variant<float, 32, 32, 512, 1, true>(),
                     tma_variant<float, 16, 32, 512, 1, true>(), tma_variant<float, 16, 16, 256, 3, true>(),
-                    tma_variant<float, 16, 32, 256, 2, true, 1>()};
+                    tma_variant<float, 16, 32, 256, 2, true, 1>(), tma_variant<float, 32, 32, 384, 1, true>(),
+                    tma_variant<float, 32, 32, 576, 1, true>()};
         return {step_variant<float, 16, 32, 512, 1>(), step_variant<float, 16, 16, 256, 2>(),
                 step_variant<float, 16, 16, 256, 3>(), step_variant<float, 16, 16, 256, 4>(),
                 step_variant<float, 8, 32, 256, 3>(),  step_variant<float, 32, 32, 512, 1>(),
                 step_variant<float, 16, 32, 512, 2>(), tma_variant<float, 32, 32, 512, 1>(),
                 tma_variant<float, 16, 32, 512, 1>(), tma_variant<float, 16, 16, 256, 3>(),
                 tma_variant<float, 8, 32, 256, 3>(), tma_variant<float, 16, 32, 256, 2, false, 1>(),
-                tma_variant<float, 32, 32, 512, 1, false, 1>()};
+                tma_variant<float, 32, 32, 512, 1, false, 1>(), tma_variant<float, 32, 32, 384, 1>(),
+                tma_variant<float, 32, 32, 576, 1>()};
     }
     static constexpr int SJ = 16, SI = 32, SNT = 256;
 };

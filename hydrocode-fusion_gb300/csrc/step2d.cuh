@@ -367,6 +367,16 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
     const int tid = threadIdx.x;
     const int m = a.m, n = a.n, slot = a.seq % 3;
     constexpr int WJ = SM::WJ, SJ = SM::SJ, SI = SM::SI;
+    // face queue and FP32 retry list (read only after the barriers below;
+    // the previous tile finished with them at its final barrier)
+    __shared__ int s_qn;
+    constexpr int RETRY_MAX = 128;  // FP32 faces whose star state failed its check, redone in FP64
+    __shared__ int s_nretry;
+    __shared__ unsigned short s_retry[RETRY_MAX];
+    if (tid == 0) {
+        s_qn = 0;
+        s_nretry = 0;
+    }
     // value (lj, li) = cell (J0-2+lj, I0-2+li)
     constexpr int WP = STAGED ? SL::BW : SM::WI;
     constexpr int WO = STAGED ? SL::X - 2 : 0;
@@ -389,14 +399,26 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
             for (int k = 0; k < 4; ++k)
                 Wx(k, lj, li) = w[k];
         }
+        __syncthreads();  // (an interior staged tile wrote nothing here)
     }
-    __syncthreads();
 
-    // 2. limited slopes of the tile and a 1-cell halo (corners are never used)
-    for (int idx = tid; idx < SJ * SI; idx += NT) {
-        int sj = idx / SI, si = idx - sj * SI;
-        if ((sj == 0 || sj == SJ - 1) && (si == 0 || si == SI - 1))
-            continue;
+    // 2. limited slopes of the tile and a 1-cell halo; the 4 corners are never
+    //    used, so the (SJ SI - 4) cells are enumerated without them: first and
+    //    last halo rows without their end cells, the SJ - 2 full rows between
+    constexpr int NSL = SJ * SI - 4;
+    for (int idx = tid; idx < NSL; idx += NT) {
+        int sj, si;
+        if (idx < SI - 2) {
+            sj = 0;
+            si = idx + 1;
+        } else if (idx < SI - 2 + (SJ - 2) * SI) {
+            const int r = idx - (SI - 2);
+            sj = 1 + r / SI;
+            si = r - (sj - 1) * SI;
+        } else {
+            sj = SJ - 1;
+            si = 1 + idx - (SI - 2) - (SJ - 2) * SI;
+        }
         int j = J0 - 1 + sj, i = I0 - 1 + si;
         const bool inside = STAGED && j >= 0 && j < m && i >= 0 && i < n;
         size_t o = slope_index(a, j, i);
@@ -419,8 +441,10 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
     }
     __syncthreads();
 
-    // 2b. ghost slopes at non-periodic domain edges
-    if (a.bx != -7) {
+    // 2b. ghost slopes at non-periodic domain edges (edge tiles only)
+    const bool ghost_x = a.bx != -7 && (J0 == 0 || m - J0 + 1 <= SJ - 1);
+    const bool ghost_y = a.by != -7 && (I0 == 0 || n - I0 + 1 <= SI - 1);
+    if (ghost_x) {
         const int sjg[2] = {(J0 == 0) ? 0 : -1, (m - J0 + 1 <= SJ - 1) ? m - J0 + 1 : -1};
         for (int idx = tid; idx < 2 * TI; idx += NT) {
             int side = idx / TI, si = 1 + idx % TI;
@@ -440,7 +464,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
                 Sx(4 + k, sj, si) = (a.bx == -1) ? R(0) : Sx(4 + k, se, si);
         }
     }
-    if (a.by != -7) {
+    if (ghost_y) {
         const int sig[2] = {(I0 == 0) ? 0 : -1, (n - I0 + 1 <= SI - 1) ? n - I0 + 1 : -1};
         for (int idx = tid; idx < 2 * TJ; idx += NT) {
             int side = idx / TJ, sj = 1 + idx % TJ;
@@ -458,7 +482,8 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
                 Sx(k, sj, si) = (a.by == -1) ? R(0) : Sx(k, sj, se);
         }
     }
-    __syncthreads();
+    if (ghost_x || ghost_y)
+        __syncthreads();
 
     // 3. faces, in two passes.  Pass A reconstructs every face: a pair within
     //    the uniform threshold (the acoustic case of the GRP solver) is
@@ -471,11 +496,6 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
     constexpr int NFX = (TJ + 1) * TI, NFY = TJ * (TI + 1), NF = NFX + NFY;
     int my_iters = 0, my_newton = 0, my_fb = 0;
     const int lane = tid & 31;
-    __shared__ int s_qn;
-    // FP32 faces whose star state failed its check, solved again in FP64 after the passes
-    constexpr int RETRY_MAX = 128;
-    __shared__ int s_nretry;
-    __shared__ unsigned short s_retry[RETRY_MAX];
     // sides of face f (x-faces first, then y-faces) in the face's normal frame;
     // false when the face lies outside the domain
     auto sides = [&](int f, Side<R>& L, Side<R>& Rr, int& lj, int& li, int& j, int& i) -> bool {
@@ -564,11 +584,6 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
             }
         }
     };
-    if (tid == 0) {
-        s_qn = 0;
-        s_nretry = 0;
-    }
-    __syncthreads();
     // pass A: warp-uniform rounds so the queue appends are warp-aggregated
     for (int fb = tid - lane; fb < NF; fb += NT) {
         const int f = fb + lane;
