@@ -203,8 +203,8 @@ BatchShape batch_shape()
 
 static const std::vector<BatchShape>& batch_shapes()
 {
-    static const std::vector<BatchShape> s = {batch_shape<32, 32, 512, 1>(), batch_shape<16, 32, 512, 1>(),
-                                              batch_shape<8, 32, 256, 3>(), batch_shape<16, 16, 256, 2>()};
+    static const std::vector<BatchShape> s = {batch_shape<32, 32, 512, 1>(), batch_shape<8, 32, 256, 3>(),
+                                              batch_shape<16, 16, 256, 4>()};
     return s;
 }
 
@@ -322,8 +322,8 @@ static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps,
             a.hy = (float)r.hy;
             a.hhx = (float)(0.5 * r.hx);
             a.hhy = (float)(0.5 * r.hy);
-            a.pow2_x = Solver2D<float>::is_pow2(r.hx);
-            a.pow2_y = Solver2D<float>::is_pow2(r.hy);
+            a.pow2_x = h_is_pow2(r.hx);
+            a.pow2_y = h_is_pow2(r.hy);
             a.inv_hx = (float)(1.0 / r.hx);
             a.inv_hy = (float)(1.0 / r.hy);
             a.alpha = (float)r.alpha;

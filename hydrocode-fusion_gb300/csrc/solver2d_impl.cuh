@@ -55,34 +55,36 @@ StepVariant<R> tma_variant()
                           (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED, STAGES>, STAGES, 0, {}};
 }
 
+// The compiled configurations, each list instantiated in its own translation
+// unit so the kernels compile in parallel (f32_gathered.cu, f32_tma.cu,
+// f32_learned.cu, f64_variants.cu).  The lists keep the configurations that
+// the autotuner picks on some workload; HYDRO_STEP_VARIANT* index into them.
+void variants_f32_gathered(std::vector<StepVariant<float>>& v);
+void variants_f32_tma(std::vector<StepVariant<float>>& v);
+void variants_f32_learned(std::vector<StepVariant<float>>& v);
+void variants_f64(std::vector<StepVariant<double>>& v);
+
 template <typename R> struct Variants;
 template <> struct Variants<double> {
     static std::vector<StepVariant<double>> all(bool)
     {
-        return {step_variant<double, 16, 16, 256, 1>(), step_variant<double, 16, 16, 256, 3>(),
-                step_variant<double, 8, 16, 128, 4>(), step_variant<double, 32, 16, 512, 1>(),
-                tma_variant<double, 16, 16, 256, 1>(),  tma_variant<double, 32, 16, 512, 1>()};
+        std::vector<StepVariant<double>> v;
+        variants_f64(v);
+        return v;
     }
     static constexpr int SJ = 16, SI = 32, SNT = 256;  // split sweeps
 };
 template <> struct Variants<float> {
     static std::vector<StepVariant<float>> all(bool learned)
     {
-        if (learned)
-            return {step_variant<float, 32, 32, 512, 1, true>(), step_variant<float, 16, 32, 512, 1, true>(),
-                    step_variant<float, 16, 32, 512, 2, true>(), step_variant<float, 16, 16, 256, 2, true>(),
-                    step_variant<float, 16, 16, 256, 3, true>(), tma_variant<float, 32, 32, 512, 1, true>(),
-                    tma_variant<float, 16, 32, 512, 1, true>(), tma_variant<float, 16, 16, 256, 3, true>(),
-                    tma_variant<float, 16, 32, 256, 2, true, 1>(), tma_variant<float, 32, 32, 384, 1, true>(),
-                    tma_variant<float, 32, 32, 576, 1, true>()};
-        return {step_variant<float, 16, 32, 512, 1>(), step_variant<float, 16, 16, 256, 2>(),
-                step_variant<float, 16, 16, 256, 3>(), step_variant<float, 16, 16, 256, 4>(),
-                step_variant<float, 8, 32, 256, 3>(),  step_variant<float, 32, 32, 512, 1>(),
-                step_variant<float, 16, 32, 512, 2>(), tma_variant<float, 32, 32, 512, 1>(),
-                tma_variant<float, 16, 32, 512, 1>(), tma_variant<float, 16, 16, 256, 3>(),
-                tma_variant<float, 8, 32, 256, 3>(), tma_variant<float, 16, 32, 256, 2, false, 1>(),
-                tma_variant<float, 32, 32, 512, 1, false, 1>(), tma_variant<float, 32, 32, 384, 1>(),
-                tma_variant<float, 32, 32, 576, 1>()};
+        std::vector<StepVariant<float>> v;
+        if (learned) {
+            variants_f32_learned(v);
+        } else {
+            variants_f32_gathered(v);
+            variants_f32_tma(v);
+        }
+        return v;
     }
     static constexpr int SJ = 16, SI = 32, SNT = 256;
 };
@@ -180,6 +182,14 @@ __global__ void k_cfl_min(const R* __restrict__ w, size_t plane, int m, int n, i
         if (lane == 0 && !(best != best))
             atomicMin(out, (unsigned long long)__double_as_longlong(best));
     }
+}
+
+// True when h is a power of two (then d/h == d*(1/h) exactly).
+inline bool h_is_pow2(double h)
+{
+    int e;
+    double f = frexp(h, &e);
+    return h > 0.0 && f == 0.5;
 }
 
 // Gas constants of the step kernels, derived once in FP64 on the host.
@@ -573,12 +583,7 @@ public:
 
     void fill_gas(Gas<R>& G, double g, double eps) { fill_gas_params(G, g, eps); }
 
-    static bool is_pow2(double h)
-    {
-        int e;
-        double f = frexp(h, &e);
-        return h > 0.0 && f == 0.5;
-    }
+    static bool is_pow2(double h) { return h_is_pow2(h); }
 
     int run(const RunConfig& rc, int split, int stats, const double* time_plot, int N_plot, int N_T,
             double** snap_out, hydro_run_info* info, int* final_nt) override
