@@ -406,7 +406,13 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
     //    used, so the (SJ SI - 4) cells are enumerated without them: first and
     //    last halo rows without their end cells, the SJ - 2 full rows between
     constexpr int NSL = SJ * SI - 4;
-    for (int idx = tid; idx < NSL; idx += NT) {
+    constexpr int ROUNDS2 = (NSL + NT - 1) / NT;
+    // constant trip count, unrolled: the rounds' loads and limiter chains interleave
+#pragma unroll
+    for (int rr = 0; rr < ROUNDS2; ++rr) {
+        const int idx = tid + rr * NT;
+        if (idx >= NSL)
+            break;
         int sj, si;
         if (idx < SI - 2) {
             sj = 0;
@@ -421,7 +427,9 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
         }
         int j = J0 - 1 + sj, i = I0 - 1 + si;
         const bool inside = STAGED && j >= 0 && j < m && i >= 0 && i < n;
-        size_t o = slope_index(a, j, i);
+        size_t o = 0;  // global index of the previous slopes, needed only when they are not staged
+        if (!inside)
+            o = slope_index(a, j, i);
         // staged previous slopes: plane k at B[(k * BJ + sj) * BW + si - 1 + X]
         const R* bs = STAGED ? B + sj * SL::BW + si - 1 + SL::X : nullptr;
 #pragma unroll
@@ -683,7 +691,12 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
 
     // 4. conservative update and new slopes
     unsigned bad = 0;
-    for (int idx = tid; idx < TJ * TI; idx += NT) {
+    constexpr int ROUNDS4 = (TJ * TI + NT - 1) / NT;
+#pragma unroll
+    for (int rr = 0; rr < ROUNDS4; ++rr) {
+        const int idx = tid + rr * NT;
+        if (idx >= TJ * TI)
+            break;
         int cj = idx / TI, ci = idx - cj * TI;
         int j = J0 + cj, i = I0 + ci;
         if (j >= m || i >= n)
