@@ -780,11 +780,22 @@ __device__ __forceinline__ int star_dire_check2(const R U[4], const R D[4], R ep
 {
     if (U[3] < eps || U[0] < eps)
         return 1;
-    if (!(M<R>::finite_(U[0]) && M<R>::finite_(U[1]) && M<R>::finite_(U[2]) && M<R>::finite_(U[3])))
-        return 2;
-    if (!(M<R>::finite_(D[0]) && M<R>::finite_(D[1]) && M<R>::finite_(D[2]) && M<R>::finite_(D[3])))
-        return 3;
-    return 0;
+    if constexpr (sizeof(R) == 4) {
+        // FP32 form: a sum of magnitudes is finite iff every term is (barring
+        // an overflow of the sum itself, which no usable state reaches): one
+        // add per value instead of an exponent test
+        if (!(fabsf(U[0]) + fabsf(U[1]) + fabsf(U[2]) + fabsf(U[3]) <= 3.402823466e38f))
+            return 2;
+        if (!(fabsf(D[0]) + fabsf(D[1]) + fabsf(D[2]) + fabsf(D[3]) <= 3.402823466e38f))
+            return 3;
+        return 0;
+    } else {
+        if (!(M<R>::finite_(U[0]) && M<R>::finite_(U[1]) && M<R>::finite_(U[2]) && M<R>::finite_(U[3])))
+            return 2;
+        if (!(M<R>::finite_(D[0]) && M<R>::finite_(D[1]) && M<R>::finite_(D[2]) && M<R>::finite_(D[3])))
+            return 3;
+        return 0;
+    }
 }
 
 // ifvar_check (dim 2), fluid_var_check.c:21-51: reconstructed positivity and
@@ -794,11 +805,19 @@ __device__ __forceinline__ bool ifvar_bad(const Side<R>& L, const Side<R>& Rr, R
 {
     if (L.p < eps || Rr.p < eps || L.rho < eps || Rr.rho < eps)
         return true;
-    bool f = M<R>::finite_(L.dp) && M<R>::finite_(Rr.dp) && M<R>::finite_(L.du) && M<R>::finite_(Rr.du) &&
-             M<R>::finite_(L.dv) && M<R>::finite_(Rr.dv) && M<R>::finite_(L.drho) && M<R>::finite_(Rr.drho) &&
-             M<R>::finite_(L.tp) && M<R>::finite_(Rr.tp) && M<R>::finite_(L.tu) && M<R>::finite_(Rr.tu) &&
-             M<R>::finite_(L.tv) && M<R>::finite_(Rr.tv) && M<R>::finite_(L.trho) && M<R>::finite_(Rr.trho);
-    return !f;
+    if constexpr (sizeof(R) == 4) {
+        // FP32 form: finiteness of all 16 slopes from one sum of magnitudes (see star_dire_check2)
+        const float s = fabsf(L.dp) + fabsf(Rr.dp) + fabsf(L.du) + fabsf(Rr.du) + fabsf(L.dv) + fabsf(Rr.dv) +
+                        fabsf(L.drho) + fabsf(Rr.drho) + fabsf(L.tp) + fabsf(Rr.tp) + fabsf(L.tu) + fabsf(Rr.tu) +
+                        fabsf(L.tv) + fabsf(Rr.tv) + fabsf(L.trho) + fabsf(Rr.trho);
+        return !(s <= 3.402823466e38f);
+    } else {
+        bool f = M<R>::finite_(L.dp) && M<R>::finite_(Rr.dp) && M<R>::finite_(L.du) && M<R>::finite_(Rr.du) &&
+                 M<R>::finite_(L.dv) && M<R>::finite_(Rr.dv) && M<R>::finite_(L.drho) && M<R>::finite_(Rr.drho) &&
+                 M<R>::finite_(L.tp) && M<R>::finite_(Rr.tp) && M<R>::finite_(L.tu) && M<R>::finite_(Rr.tu) &&
+                 M<R>::finite_(L.tv) && M<R>::finite_(Rr.tv) && M<R>::finite_(L.trho) && M<R>::finite_(Rr.trho);
+        return !f;
+    }
 }
 
 }  // namespace hydro
