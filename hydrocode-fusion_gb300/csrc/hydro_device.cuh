@@ -54,9 +54,28 @@ template <> struct M<float> {
 // ---------------------------------------------------------------------------
 // minmod limiters (tools.h:44-73)
 // ---------------------------------------------------------------------------
+// FP32 form: the same values without branches.  When the arguments share a
+// sign (the only case that does not return 0), the reference's comparison
+// sequence returns the argument of smallest magnitude, i.e. the minimum of
+// positive or the maximum of negative arguments; fminf/fmaxf return that
+// argument exactly.  (They differ from the sequence only for NaN arguments,
+// which the reconstruction check rejects anyway.)
+__device__ __forceinline__ float minmod2_sel(float sL, float sR)
+{
+    const float r = sR > 0.f ? fminf(sL, sR) : fmaxf(sL, sR);
+    return sL * sR <= 0.f ? 0.f : r;
+}
+__device__ __forceinline__ float minmod3_sel(float sL, float sR, float sm)
+{
+    const float r = sm > 0.f ? fminf(fminf(sL, sR), sm) : fmaxf(fmaxf(sL, sR), sm);
+    return (sL * sm <= 0.f || sR * sm <= 0.f) ? 0.f : r;
+}
+
 template <typename R>
 __device__ __forceinline__ R minmod2(R sL, R sR)
 {
+    if constexpr (sizeof(R) == 4)
+        return minmod2_sel(sL, sR);
     if (sL * sR <= R(0))
         return R(0);
     if (sR > R(0) && sR < sL)
@@ -69,6 +88,8 @@ __device__ __forceinline__ R minmod2(R sL, R sR)
 template <typename R>
 __device__ __forceinline__ R minmod3(R sL, R sR, R sm)
 {
+    if constexpr (sizeof(R) == 4)
+        return minmod3_sel(sL, sR, sm);
     if (sL * sm <= R(0) || sR * sm <= R(0))
         return R(0);
     if (sm > R(0) && sm < sL && sm < sR)
