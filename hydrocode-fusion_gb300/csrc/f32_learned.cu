@@ -5,11 +5,12 @@ namespace hydro {
 
 void variants_f32_learned(std::vector<StepVariant<float>>& v)
 {
-    v.push_back(step_variant<float, 32, 32, 512, 1, true>());
-    v.push_back(step_variant<float, 16, 32, 512, 2, true>());
+    // the TMA-staged kernels first: index 0 is the default when nothing is tuned
     v.push_back(tma_variant<float, 32, 32, 512, 1, true>());
     v.push_back(tma_variant<float, 32, 32, 384, 1, true>());
     v.push_back(tma_variant<float, 16, 32, 256, 2, true, 1>());
+    v.push_back(step_variant<float, 32, 32, 512, 1, true>());
+    v.push_back(step_variant<float, 16, 32, 512, 2, true>());
 }
 
 }  // namespace hydro

@@ -81,8 +81,9 @@ template <> struct Variants<float> {
         if (learned) {
             variants_f32_learned(v);
         } else {
-            variants_f32_gathered(v);
+            // the TMA-staged kernels first: index 0 is the default when nothing is tuned
             variants_f32_tma(v);
+            variants_f32_gathered(v);
         }
         return v;
     }
