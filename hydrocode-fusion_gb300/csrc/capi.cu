@@ -36,6 +36,21 @@ bool cuda_ok(cudaError_t e, const char* what)
     return false;
 }
 
+bool pageable_host_access()
+{
+    if (const char* e = getenv("HYDRO_STAGED_HOST_COPY"))
+        if (atoi(e) != 0)
+            return false;
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return false;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return v == 1;
+}
+
 RunConfig run_config_from(const double* cfg, int ncfg)
 {
     auto at = [&](int k) { return k < ncfg ? cfg[k] : INFINITY; };
@@ -200,16 +215,26 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
         exit(5);
     }
     size_t mn = (size_t)m * n;
-    std::vector<double> host(5 * mn);
-    double* pl[5] = {&host[0], &host[mn], &host[2 * mn], &host[3 * mn], &host[4 * mn]};
-    for (int j = 0; j < m; ++j) {
-        memcpy(pl[0] + (size_t)j * n, CV[0].RHO[j], n * sizeof(double));
-        memcpy(pl[1] + (size_t)j * n, CV[0].U[j], n * sizeof(double));
-        memcpy(pl[2] + (size_t)j * n, CV[0].V[j], n * sizeof(double));
-        memcpy(pl[3] + (size_t)j * n, CV[0].P[j], n * sizeof(double));
-        memcpy(pl[4] + (size_t)j * n, CV[0].E[j], n * sizeof(double));
+    // The caller's state is a set of separately allocated rows.  Where the GPU
+    // reads pageable host memory coherently (Grace-Blackwell), the kernels
+    // gather and scatter those rows themselves; elsewhere the rows are packed
+    // into one host buffer and copied.
+    const bool direct = pageable_host_access();
+    std::vector<double> host(direct ? 0 : 5 * mn);
+    double* pl[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (!direct) {
+        for (int k = 0; k < 5; ++k)
+            pl[k] = &host[(size_t)k * mn];
+        for (int j = 0; j < m; ++j) {
+            memcpy(pl[0] + (size_t)j * n, CV[0].RHO[j], n * sizeof(double));
+            memcpy(pl[1] + (size_t)j * n, CV[0].U[j], n * sizeof(double));
+            memcpy(pl[2] + (size_t)j * n, CV[0].V[j], n * sizeof(double));
+            memcpy(pl[3] + (size_t)j * n, CV[0].P[j], n * sizeof(double));
+            memcpy(pl[4] + (size_t)j * n, CV[0].E[j], n * sizeof(double));
+        }
     }
-    if (s->upload(pl[0], pl[1], pl[2], pl[3], pl[4], config[6])) {
+    const double* const* in_rows[5] = {CV[0].RHO, CV[0].U, CV[0].V, CV[0].P, CV[0].E};
+    if (direct ? s->upload_rows(in_rows) : s->upload(pl[0], pl[1], pl[2], pl[3], pl[4], config[6])) {
         fprintf(stderr, "hydro_gb300: upload failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }
@@ -226,7 +251,8 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
         fprintf(stderr, "hydro_gb300: time loop failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }
-    if (s->download(pl[0], pl[1], pl[2], pl[3], pl[4])) {
+    double* const* out_rows[5] = {CV[nt].RHO, CV[nt].U, CV[nt].V, CV[nt].P, CV[nt].E};
+    if (direct ? s->download_rows(out_rows) : s->download(pl[0], pl[1], pl[2], pl[3], pl[4])) {
         fprintf(stderr, "hydro_gb300: download failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }
@@ -242,7 +268,8 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
     };
     for (int k = 1; k < nt; ++k)  // CV[0] already holds the initial data
         scatter(k, snaps[k].data());
-    scatter(nt, host.data());
+    if (!direct)
+        scatter(nt, host.data());
 
     if (info.halted == 1)
         printf("Error on the time step %d (x-face code %d, y-face code %d); the step was discarded.\n", info.k_out,

@@ -56,6 +56,11 @@ public:
     virtual int upload(const double* rho, const double* u, const double* v, const double* p, const double* E,
                        double gamma) = 0;
     virtual int download(double* rho, double* u, double* v, double* p, double* E) = 0;
+    // The same from/to the caller's row arrays (rows[k][j] = row j of field k:
+    // rho, u, v, p, E), read and written by the GPU itself; only where the
+    // device accesses pageable host memory coherently (pageable_host_access()).
+    virtual int upload_rows(const double* const* const rows[5]) = 0;
+    virtual int download_rows(double* const* const rows[5]) = 0;
     // Runs the plan; snapshots (if any) are written as 5 x-major planes
     // (rho,u,v,p,E) each into snap_out[nt] (host memory, may be null).
     virtual int run(const RunConfig& rc, int split, int stats, const double* time_plot, int N_plot, int N_T,
@@ -72,6 +77,11 @@ public:
 
 Solver2DBase* make_solver2d_f64(int m, int n);
 Solver2DBase* make_solver2d_f32(int m, int n, int learned);
+
+// True when the current device reads and writes pageable host memory
+// coherently (Grace-Blackwell address translation), so kernels may take the
+// caller's malloc'd arrays directly; HYDRO_STAGED_HOST_COPY=1 turns it off.
+bool pageable_host_access();
 
 // error reporting + launch counting shared by all TUs
 void set_error(const std::string& msg);

@@ -117,6 +117,26 @@ __global__ void k_unpack_plane(const R* __restrict__ in, double* __restrict__ ou
     }
 }
 
+// Gather of one field from the caller's row arrays in host memory (read by
+// the GPU through coherent pageable-memory access): row j at rows[j].
+template <typename R>
+__global__ void k_gather_rows(const double* const* __restrict__ rows, R* __restrict__ out, int m, int n, int ld)
+{
+    const int j = blockIdx.y;
+    const double* __restrict__ r = rows[j];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[(size_t)j * ld + i] = (R)r[i];
+}
+
+template <typename R>
+__global__ void k_scatter_rows(const R* __restrict__ in, double* const* __restrict__ rows, int m, int n, int ld)
+{
+    const int j = blockIdx.y;
+    double* __restrict__ r = rows[j];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        r[i] = (double)in[(size_t)j * ld + i];
+}
+
 // E = 0.5 u^2 + p/(gamma-1)/rho; E += 0.5 v^2 (the driver's formula,
 // src/hydrocode_2D/hydrocode.c:252-253), evaluated in FP64.
 static __global__ void k_energy(const double* rho, const double* u, const double* v, const double* p, double* E, size_t total,
@@ -483,6 +503,29 @@ public:
     {
         double* dst[5] = {rho, u, v, p, E};
         return download_planes(cur_w, dst);
+    }
+
+    int upload_rows(const double* const* const rows[5]) override
+    {
+        const dim3 grid((n + 255) / 256 < 4 ? (n + 255) / 256 : 4, m);
+        for (int k = 0; k < 5; ++k) {
+            k_gather_rows<R><<<grid, 256, 0, stream>>>(rows[k], W(0) + k * plane, m, n, ld);
+            count_launch();
+        }
+        if (!cuda_ok(cudaMemsetAsync(Sx(0), 0, sizeof(R) * 8 * plane, stream), "clear")) return -1;
+        if (!cuda_ok(cudaMemsetAsync(Sx(1), 0, sizeof(R) * 8 * plane, stream), "clear")) return -1;
+        cur_w = cur_s = cur_t = 0;
+        return cuda_ok(cudaStreamSynchronize(stream), "row upload") ? 0 : -1;
+    }
+
+    int download_rows(double* const* const rows[5]) override
+    {
+        const dim3 grid((n + 255) / 256 < 4 ? (n + 255) / 256 : 4, m);
+        for (int k = 0; k < 5; ++k) {
+            k_scatter_rows<R><<<grid, 256, 0, stream>>>(W(cur_w) + k * plane, rows[k], m, n, ld);
+            count_launch();
+        }
+        return cuda_ok(cudaStreamSynchronize(stream), "row download") ? 0 : -1;
     }
 
     int conservation(double hx, double hy, double* out4) override

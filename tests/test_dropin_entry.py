@@ -14,7 +14,7 @@ TOL = 1e-12
 
 
 @pytest.mark.gpu
-def test_2d_entry_with_plot_snapshots(gpu_lib):
+def test_2d_entry_with_plot_snapshots(gpu_lib, host_path):
     hg = gpu_lib
     d = np.load(os.path.join(GOLD, "runs_2d.npz"))
     rho, u, v, p = d["snap/in"]
@@ -28,9 +28,21 @@ def test_2d_entry_with_plot_snapshots(gpu_lib):
             assert rel_l1(data[k, f], snaps[k, f]) <= TOL, (k, f)
 
 
+@pytest.fixture(params=["direct", "staged"])
+def host_path(request, monkeypatch):
+    """Both ways the scheme call moves the caller's rows: read and written by
+    the GPU itself (where it accesses pageable host memory coherently) and
+    packed into one host buffer and copied."""
+    if request.param == "staged":
+        monkeypatch.setenv("HYDRO_STAGED_HOST_COPY", "1")
+    else:
+        monkeypatch.delenv("HYDRO_STAGED_HOST_COPY", raising=False)
+    return request.param
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("split", [0, 1])
-def test_2d_entry_matches_oracle(gpu_lib, port, split):
+def test_2d_entry_matches_oracle(gpu_lib, port, split, host_path):
     hg = gpu_lib
     from hydro_gb300 import cases
 
