@@ -50,6 +50,8 @@ struct BatchDev {
     unsigned int* bar_gen;        // grid barrier: generation
     int* bar_err;                 // set when a barrier wait gave up
     unsigned long long wait_ns;   // barrier wait limit
+    Gas<float> G;                 // gas constants (one gas for the whole batch): read from the
+                                  // kernel's parameter space, not from the per-tile copy
 };
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -140,7 +142,7 @@ __device__ __forceinline__ void batch_tile(const BatchDev& B, int t, int step, S
     int lt;
     if (batch_tile_args(B, t, step, sa, lt)) {
         const int nty = B.tiles_y[B.tile_prob[t]];
-        unsplit_tile<float, TJ, TI, NT, false>(sa, (lt % nty) * TI, (lt / nty) * TJ, smem, M);
+        unsplit_tile<float, TJ, TI, NT, false>(sa, B.G, (lt % nty) * TI, (lt / nty) * TJ, smem, M);
     }
 }
 
@@ -615,6 +617,10 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
     B.bar_gen = b->sync + 3;
     B.bar_err = (int*)(b->sync + 4);
     B.wait_ns = (unsigned long long)(b->wait_s * 1e9);
+    {
+        const RunConfig rc = run_config_from(cfg, ncfg);
+        fill_gas_params(B.G, rc.gamma, rc.eps);
+    }
     if (!cuda_ok(cudaMemsetAsync(b->ctl, 0, sizeof(Ctl) * b->nprob, b->stream), "batch control clear") ||
         !cuda_ok(cudaMemsetAsync(b->sync, 0, sizeof(unsigned int) * 8, b->stream), "batch barrier clear"))
         return -1;

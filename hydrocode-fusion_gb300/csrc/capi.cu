@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -38,9 +39,12 @@ bool cuda_ok(cudaError_t e, const char* what)
 
 bool pageable_host_access()
 {
-    if (const char* e = getenv("HYDRO_STAGED_HOST_COPY"))
-        if (atoi(e) != 0)
-            return false;
+    // measured on GB300 + Grace: a 4096^2 state moves faster staged (host
+    // gather + one copy per field) than read row by row by the GPU, so the
+    // direct path is opt-in
+    const char* e = getenv("HYDRO_DIRECT_HOST_ROWS");
+    if (!e || atoi(e) == 0)
+        return false;
     int dev = 0, v = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)
         return false;
@@ -203,6 +207,28 @@ static Solver2DBase* make_solver(int m, int n, int form)
     }
 }
 
+// Runs fn(j0, j1) over row blocks of an m x n host copy on several host
+// threads when the copy is large (the caller's rows are separate allocations,
+// so the packing into and out of one buffer is plain memory traffic).
+template <typename F>
+static void parallel_rows(int m, int n, F fn)
+{
+    const size_t bytes = (size_t)m * n * 40;
+    unsigned hw = std::thread::hardware_concurrency();
+    int T = bytes < (size_t)(64u << 20) ? 1 : (int)(hw ? (hw < 16 ? hw : 16) : 4);
+    if (T > m)
+        T = m;
+    if (T <= 1) {
+        fn(0, m);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t)
+        th.emplace_back([&, t] { fn((int)((long long)m * t / T), (int)((long long)m * (t + 1) / T)); });
+    for (auto& x : th)
+        x.join();
+}
+
 // Shared body of the two 2D scheme entry points.
 static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, double* cpu_time, int N_T, int* N_plot,
                          double time_plot[], int split)
@@ -225,13 +251,15 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
     if (!direct) {
         for (int k = 0; k < 5; ++k)
             pl[k] = &host[(size_t)k * mn];
-        for (int j = 0; j < m; ++j) {
-            memcpy(pl[0] + (size_t)j * n, CV[0].RHO[j], n * sizeof(double));
-            memcpy(pl[1] + (size_t)j * n, CV[0].U[j], n * sizeof(double));
-            memcpy(pl[2] + (size_t)j * n, CV[0].V[j], n * sizeof(double));
-            memcpy(pl[3] + (size_t)j * n, CV[0].P[j], n * sizeof(double));
-            memcpy(pl[4] + (size_t)j * n, CV[0].E[j], n * sizeof(double));
-        }
+        parallel_rows(m, n, [&](int j0, int j1) {
+            for (int j = j0; j < j1; ++j) {
+                memcpy(pl[0] + (size_t)j * n, CV[0].RHO[j], n * sizeof(double));
+                memcpy(pl[1] + (size_t)j * n, CV[0].U[j], n * sizeof(double));
+                memcpy(pl[2] + (size_t)j * n, CV[0].V[j], n * sizeof(double));
+                memcpy(pl[3] + (size_t)j * n, CV[0].P[j], n * sizeof(double));
+                memcpy(pl[4] + (size_t)j * n, CV[0].E[j], n * sizeof(double));
+            }
+        });
     }
     const double* const* in_rows[5] = {CV[0].RHO, CV[0].U, CV[0].V, CV[0].P, CV[0].E};
     if (direct ? s->upload_rows(in_rows) : s->upload(pl[0], pl[1], pl[2], pl[3], pl[4], config[6])) {
@@ -258,13 +286,15 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
     }
     delete s;
     auto scatter = [&](int k, const double* src) {
-        for (int j = 0; j < m; ++j) {
-            memcpy(CV[k].RHO[j], src + (size_t)j * n, n * sizeof(double));
-            memcpy(CV[k].U[j], src + mn + (size_t)j * n, n * sizeof(double));
-            memcpy(CV[k].V[j], src + 2 * mn + (size_t)j * n, n * sizeof(double));
-            memcpy(CV[k].P[j], src + 3 * mn + (size_t)j * n, n * sizeof(double));
-            memcpy(CV[k].E[j], src + 4 * mn + (size_t)j * n, n * sizeof(double));
-        }
+        parallel_rows(m, n, [&](int j0, int j1) {
+            for (int j = j0; j < j1; ++j) {
+                memcpy(CV[k].RHO[j], src + (size_t)j * n, n * sizeof(double));
+                memcpy(CV[k].U[j], src + mn + (size_t)j * n, n * sizeof(double));
+                memcpy(CV[k].V[j], src + 2 * mn + (size_t)j * n, n * sizeof(double));
+                memcpy(CV[k].P[j], src + 3 * mn + (size_t)j * n, n * sizeof(double));
+                memcpy(CV[k].E[j], src + 4 * mn + (size_t)j * n, n * sizeof(double));
+            }
+        });
     };
     for (int k = 1; k < nt; ++k)  // CV[0] already holds the initial data
         scatter(k, snaps[k].data());

@@ -78,9 +78,9 @@ public:
 Solver2DBase* make_solver2d_f64(int m, int n);
 Solver2DBase* make_solver2d_f32(int m, int n, int learned);
 
-// True when the current device reads and writes pageable host memory
-// coherently (Grace-Blackwell address translation), so kernels may take the
-// caller's malloc'd arrays directly; HYDRO_STAGED_HOST_COPY=1 turns it off.
+// True when HYDRO_DIRECT_HOST_ROWS=1 asks for it and the current device reads
+// and writes pageable host memory coherently (Grace-Blackwell address
+// translation), so kernels may take the caller's malloc'd rows directly.
 bool pageable_host_access();
 
 // error reporting + launch counting shared by all TUs

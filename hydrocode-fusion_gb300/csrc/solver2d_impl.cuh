@@ -507,7 +507,8 @@ public:
 
     int upload_rows(const double* const* const rows[5]) override
     {
-        const dim3 grid((n + 255) / 256 < 4 ? (n + 255) / 256 : 4, m);
+        // one element per thread: host-memory latency is hidden by having every load in flight
+        const dim3 grid((n + 255) / 256, m);
         for (int k = 0; k < 5; ++k) {
             k_gather_rows<R><<<grid, 256, 0, stream>>>(rows[k], W(0) + k * plane, m, n, ld);
             count_launch();
@@ -520,7 +521,7 @@ public:
 
     int download_rows(double* const* const rows[5]) override
     {
-        const dim3 grid((n + 255) / 256 < 4 ? (n + 255) / 256 : 4, m);
+        const dim3 grid((n + 255) / 256, m);
         for (int k = 0; k < 5; ++k) {
             k_scatter_rows<R><<<grid, 256, 0, stream>>>(W(cur_w) + k * plane, rows[k], m, n, ld);
             count_launch();

@@ -250,21 +250,21 @@ static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, c
 // Solve one face given its two sides in the face's normal frame (KNOWN as in
 // q1d_star: whether the uniform-pair decision has already been made).
 template <typename R, int KNOWN = 0>
-__device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, const StepArgs<R>& a, FaceOut<R>& o,
-                                          int& iters, int& fallback, bool ydir, R p_start = R(-1))
+__device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, R tau, R htau,
+                                          FaceOut<R>& o, int& iters, int& fallback, bool ydir, R p_start = R(-1))
 {
-    int code = ifvar_bad(L, Rr, a.G.eps) ? 1 : 0;
+    int code = ifvar_bad(L, Rr, G.eps) ? 1 : 0;
     Star<R> S;
     StarInfo st;
     st.fallback = 0;
-    q1d_star<R, KNOWN>(L, Rr, a.G, S, st, p_start);
+    q1d_star<R, KNOWN>(L, Rr, G, S, st, p_start);
     R D[4], U[4];
-    q1d_derivs<R, KNOWN>(L, Rr, a.G, S, D, U);
+    q1d_derivs<R, KNOWN>(L, Rr, G, S, D, U);
     iters = st.iters;
     fallback = st.fallback;
-    if (star_dire_check2(U, D, a.G.eps))
+    if (star_dire_check2(U, D, G.eps))
         code = 2;
-    face_flux<R>(D, U, a.tau, a.htau, a.G, o, ydir);
+    face_flux<R>(D, U, tau, htau, G, o, ydir);
     return code;
 }
 
@@ -357,7 +357,8 @@ struct StageLayout {
 //     (rows J0-1.., same columns) at B; only the ghost cells of tiles at the
 //     domain edge are gathered.  FX may alias B (B is dead after phase 2).
 template <typename R, int TJ, int TI, int NT, bool LEARNED, bool STAGED>
-__device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, const int J0, R* __restrict__ W,
+__device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
+                                          R* __restrict__ W,
                                           const R* B, R* __restrict__ S, R* FX, R* __restrict__ FY,
                                           unsigned short* __restrict__ Q, float* __restrict__ P,
                                           const MlpShared& Mlp)
@@ -562,7 +563,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
         const bool ydir = f >= NFX;
         FaceOut<R> o;
         int it, fbk;
-        int code = solve_face<R, decltype(known)::value>(L, Rr, a, o, it, fbk, ydir, p_start);
+        int code = solve_face<R, decltype(known)::value>(L, Rr, G, a.tau, a.htau, o, it, fbk, ydir, p_start);
         if (it >= 0) {
             my_newton++;
             my_iters += it;
@@ -598,7 +599,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
         Side<R> L, Rr;
         int lj = 0, li = 0, j = 0, i = 0;
         const bool active = f < NF && sides(f, L, Rr, lj, li, j, i);
-        const bool uni = active && face_uniform<R>(L, Rr, a.G);
+        const bool uni = active && face_uniform<R>(L, Rr, G);
         const bool need = active && !uni;
         const unsigned want = __ballot_sync(0xffffffffu, need);
         if (want) {
@@ -625,7 +626,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
             Side<R> L, Rr;
             int lj = 0, li = 0, j = 0, i = 0;
             sides(act ? (int)Q[q] : 0, L, Rr, lj, li, j, i);
-            const R g = learned_guess_any<R>(L, Rr, act, a.G, Mlp);
+            const R g = learned_guess_any<R>(L, Rr, act, G, Mlp);
             if (act)
                 P[q] = (float)g;
         }
@@ -668,7 +669,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
                 sides(f, L, Rr, lj, li, j, i);
                 FaceOut<R> o;
                 const bool ydir = f >= NFX;
-                const int code = solve_face_fp64_retry(L, Rr, a.G.g64, a.G.eps64, (double)a.tau, ydir, o);
+                const int code = solve_face_fp64_retry(L, Rr, G.g64, G.eps64, (double)a.tau, ydir, o);
                 if (!ydir) {
                     report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
 #pragma unroll
@@ -713,8 +714,8 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
         R ene = rho * E - a.nu * (FXx(3, cj + 1, ci) - FXx(3, cj, ci)) - a.mu * (FYx(3, cj, ci + 1) - FYx(3, cj, ci));
         rho += -a.nu * (FXx(0, cj + 1, ci) - FXx(0, cj, ci)) - a.mu * (FYx(0, cj, ci + 1) - FYx(0, cj, ci));
         R un = mom_x / rho, vn = mom_y / rho, En = ene / rho;
-        R pn = (ene - R(0.5) * mom_x * un - R(0.5) * mom_y * vn) * a.G.gm1;
-        if (pn < a.G.eps || rho < a.G.eps)
+        R pn = (ene - R(0.5) * mom_x * un - R(0.5) * mom_y * vn) * G.gm1;
+        if (pn < G.eps || rho < G.eps)
             bad = 1;
         a.dst_w[o] = rho;
         a.dst_w[a.plane + o] = un;
@@ -738,8 +739,8 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const int I0, co
 
 // The gathered tile with its shared-memory carve-up (W | S | FX | FY).
 template <typename R, int TJ, int TI, int NT, bool LEARNED>
-__device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0, const int J0, unsigned char* smem_raw,
-                                             const MlpShared& Mlp)
+__device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
+                                             unsigned char* smem_raw, const MlpShared& Mlp)
 {
     using SM = UnsplitSmem<R, TJ, TI>;
     R* W = reinterpret_cast<R*>(smem_raw);
@@ -748,7 +749,7 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const int I0,
     R* FY = FX + SM::nFX;
     unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + SM::bytes_f);
     float* P = LEARNED ? reinterpret_cast<float*>(smem_raw + SM::p_off) : nullptr;
-    tile_body<R, TJ, TI, NT, LEARNED, false>(a, I0, J0, W, nullptr, S, FX, FY, Q, P, Mlp);
+    tile_body<R, TJ, TI, NT, LEARNED, false>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, P, Mlp);
 }
 
 template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
@@ -761,7 +762,7 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
     MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + SM::mlp_off);
     if (LEARNED)
         mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
-    unsplit_tile<R, TJ, TI, NT, LEARNED>(a, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
+    unsplit_tile<R, TJ, TI, NT, LEARNED>(a, a.G, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
 }
 
 // ---------------------------------------------------------------------------
@@ -870,7 +871,7 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
         unsigned char* cur = smem_raw + stg * SL::bytes;
         R* W = reinterpret_cast<R*>(cur + SL::a_off);
         R* B = reinterpret_cast<R*>(cur + SL::b_off);
-        tile_body<R, TJ, TI, NT, LEARNED, true>(a, (t % nti) * TI, (t / nti) * TJ, W, B, S, B, FY, Q, P, Mlp);
+        tile_body<R, TJ, TI, NT, LEARNED, true>(a, a.G, (t % nti) * TI, (t / nti) * TJ, W, B, S, B, FY, Q, P, Mlp);
     }
     if (failed && threadIdx.x == 0) {
         // let the copies still in flight land (bounded) before the CTA exits, then report
@@ -1001,7 +1002,7 @@ __global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R
         FaceOut<R> o;
         int it;
         int fbk;
-        const int code = solve_face<R>(L, Rr, a, o, it, fbk, YDIR != 0);
+        const int code = solve_face<R>(L, Rr, a.G, a.tau, a.htau, o, it, fbk, YDIR != 0);
         if (it >= 0) {
             my_newton++;
             my_iters += it;

@@ -30,13 +30,14 @@ def test_2d_entry_with_plot_snapshots(gpu_lib, host_path):
 
 @pytest.fixture(params=["direct", "staged"])
 def host_path(request, monkeypatch):
-    """Both ways the scheme call moves the caller's rows: read and written by
-    the GPU itself (where it accesses pageable host memory coherently) and
-    packed into one host buffer and copied."""
-    if request.param == "staged":
-        monkeypatch.setenv("HYDRO_STAGED_HOST_COPY", "1")
+    """Both ways the scheme call moves the caller's rows: packed into one host
+    buffer and copied (the default), and read and written by the GPU itself
+    (HYDRO_DIRECT_HOST_ROWS=1, where it accesses pageable host memory
+    coherently)."""
+    if request.param == "direct":
+        monkeypatch.setenv("HYDRO_DIRECT_HOST_ROWS", "1")
     else:
-        monkeypatch.delenv("HYDRO_STAGED_HOST_COPY", raising=False)
+        monkeypatch.delenv("HYDRO_DIRECT_HOST_ROWS", raising=False)
     return request.param
 
 
