@@ -4,8 +4,10 @@
 // pitched planes), boundary table, time step and halting control block.  All
 // tiles of all problems form one flat work list, and every tile runs exactly
 // the per-tile code of the one-problem FP32 step (unsplit_tile), so each
-// problem's result is bit-identical to a one-problem FP32 run of the same
-// data.  There is no reference counterpart: the reference advances one grid
+// problem's result is a one-problem FP32 run of the same data (to the last
+// bit where the same compiled instance runs; separately compiled kernels may
+// contract multiply-adds differently under fast math, a difference at FP32
+// rounding).  There is no reference counterpart: the reference advances one grid
 // per process (grp_solver_2D_EUL_source.c:146-286).
 //
 // Schedules (picked by hydro_batch_autotune from timings on the real batch):
@@ -146,7 +148,9 @@ __device__ __forceinline__ void batch_tile(const BatchDev& B, int t, int step, S
     }
 }
 
-// ONE cooperative kernel for all steps of all problems.
+// ONE cooperative kernel for all steps of all problems.  The schedule only
+// decides which tile comes next; the tile code has a single call site, so
+// both schedules run the same compiled instructions.
 template <int TJ, int TI, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_batch_persistent(const __grid_constant__ BatchDev B)
 {
@@ -155,25 +159,23 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_persistent(const __grid_cons
     __shared__ int s_k;
     const MlpShared& M = *reinterpret_cast<const MlpShared*>(smem_raw);  // not read by the plain form
     for (int step = 1; step <= B.steps; ++step) {
-        if (B.dynamic) {
-            unsigned int* ctr = B.work + (step & 1);
-            for (;;) {
-                if (threadIdx.x == 0)
-                    s_k = (int)atomicAdd(ctr, 1u);
-                __syncthreads();
-                const int k = s_k;
-                __syncthreads();
-                if (k >= B.ntiles)
-                    break;
-                batch_tile<TJ, TI, NT>(B, B.order[k], step, sa, smem_raw, M);
-            }
-            // the counter of the next step was last used two steps ago: reset it
-            if (blockIdx.x == 0 && threadIdx.x == 0)
-                B.work[(step + 1) & 1] = 0u;
-        } else {
-            for (int k = blockIdx.x; k < B.ntiles; k += gridDim.x)
-                batch_tile<TJ, TI, NT>(B, B.order[k], step, sa, smem_raw, M);
-        }
+        unsigned int* ctr = B.work + (step & 1);
+        // next flat tile: the CTA's own stride (static) or the step's shared counter (dynamic)
+        auto next = [&](int k) -> int {
+            if (!B.dynamic)
+                return k + (int)gridDim.x;
+            if (threadIdx.x == 0)
+                s_k = (int)atomicAdd(ctr, 1u);
+            __syncthreads();
+            const int r = s_k;
+            __syncthreads();
+            return r;
+        };
+        for (int k = B.dynamic ? next(0) : (int)blockIdx.x; k < B.ntiles; k = next(k))
+            batch_tile<TJ, TI, NT>(B, B.order[k], step, sa, smem_raw, M);
+        // the counter of the next step was last used two steps ago: reset it
+        if (B.dynamic && blockIdx.x == 0 && threadIdx.x == 0)
+            B.work[(step + 1) & 1] = 0u;
         if (!grid_barrier(B))
             return;
     }

@@ -73,9 +73,12 @@ def test_batch_against_fp64_oracle(gpu_lib, port):
 
 @pytest.mark.gpu
 def test_batch_schedules_and_shapes_agree(gpu_lib):
-    """Same shape: every schedule gives bit-identical results (each tile is
-    computed once per step from the previous step's state, in any order).
-    Different shapes agree to FP32 rounding."""
+    """Each tile is computed once per step from the previous step's state, in
+    any order, so the order cannot change a result: the persistent schedules
+    (0-3, one compiled kernel whatever the tile order) agree bit for bit and
+    a repeated run reproduces itself bit for bit; the per-step kernel (4) and
+    other tile shapes are separately compiled instances of the same code and
+    agree to FP32 rounding."""
     hg = gpu_lib
     probs = _problems(hg)
     cfg = _cfg(hg, bx=-7, by=-2)
@@ -86,12 +89,19 @@ def test_batch_schedules_and_shapes_agree(gpu_lib):
         for sc in range(len(hg.SCHEDULES)):
             got, info, _ = _run_batch(hg, probs, cfg, sh, sc)
             assert info.schedule == sc and info.shape == sh
+            again, _, _ = _run_batch(hg, probs, cfg, sh, sc)
+            for k in range(len(SIZES)):
+                for f in FIELDS:
+                    assert np.array_equal(got[k][f], again[k][f]), ("repeat", sh, sc, k, f)
             if first is None:
                 first = got
             else:
                 for k in range(len(SIZES)):
                     for f in FIELDS:
-                        assert np.array_equal(got[k][f], first[k][f]), (sh, sc, k, f)
+                        if sc < 4:
+                            assert np.array_equal(got[k][f], first[k][f]), (sh, sc, k, f)
+                        else:
+                            assert rel_l1(got[k][f], first[k][f]) <= 1e-6, (sh, sc, k, f)
         if base is None:
             base = first
         else:
