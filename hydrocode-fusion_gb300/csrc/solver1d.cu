@@ -2,16 +2,21 @@
 //
 // A 1D tube (the benchmark tube has 400 cells) is far too small to fill a
 // GB300, and its time step depends on every interface's reconstructed state
-// each step, so the whole time loop runs inside ONE persistent CTA of 512
-// threads: the CFL minimum is a warp-shuffle + shared-memory reduction, the
-// stop/abort decisions are block-uniform, and nothing returns to the host
-// until the run ends.  State lives in global memory (L2-resident at this size).
+// each step, so the whole time loop runs inside ONE kernel launch and nothing
+// returns to the host until the run ends.  The work of a step is spread over
+// a thread-block cluster of up to 16 CTAs on as many SMs (the exact Riemann
+// solver's FP64 Newton iteration is the cost, and one SM's FP64 pipe would
+// serialise it); phases are separated by cluster barriers, the CFL minimum
+// and the stop/abort flags are reduced per CTA and then across the cluster
+// through distributed shared memory, so every CTA takes the same decisions.
+// State lives in global memory (L2-resident at this size).
 //
 // Follows Godunov_solver_EUL_source (src/finite_volume/godunov_solver_EUL_source.c:27-230)
 // and GRP_solver_EUL_source (src/finite_volume/grp_solver_EUL_source.c:27-334)
 // with bound_cond_slope_limiter (src/inter_process/bound_cond_slope_limiter.c:30-136)
 // and minmod_limiter (src/inter_process/slope_limiter.c:31-83).  Compiled with
 // --fmad=false: FP64 operations round as the reference's C code.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -42,9 +47,18 @@ struct Run1DArgs {
 
 __device__ __forceinline__ double dh(double d, const Run1DArgs& a) { return a.pow2 ? d * a.inv_h : d / a.h; }
 
+namespace cg = cooperative_groups;
+
 __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs a)
 {
-    const int m = a.m, tid = threadIdx.x, NT = blockDim.x;
+    cg::cluster_group cl = cg::this_cluster();
+    const int m = a.m, tid = threadIdx.x;
+    const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
+    // cells and faces are spread over every thread of the cluster
+    const int gtid = rank * (int)blockDim.x + tid, GNT = CL * (int)blockDim.x;
+    // per-CTA partials of the reductions, double-buffered by step parity
+    __shared__ double part_hs[2];
+    __shared__ int part_fl[2], part_bad[2];
     const double gamma = a.G.g, eps = a.eps;
     double* rho = a.cur;
     double* uu = a.cur + m;
@@ -69,7 +83,7 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
     for (k = 1; k <= a.N; ++k) {
         // plot snapshot: the reference copies CV.*[nt] to CV.*[nt+1] and continues there
         if (time_c >= a.time_plot[nt] && nt < (a.n_plot - 1)) {
-            for (int q = tid; q < 4 * m; q += NT)
+            for (int q = gtid; q < 4 * m; q += GNT)
                 a.snaps[(size_t)nt * 4 * m + q] = a.cur[q];
             nt++;
         }
@@ -109,7 +123,7 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
         }
         __syncthreads();
         if (a.order == 2) {
-            for (int j = tid; j < m; j += NT) {
+            for (int j = gtid; j < m; j += GNT) {
                 const double* U3[3] = {uu, pp, rho};
                 double* S3[3] = {s_u, s_p, s_rho};
                 const double ULq[3] = {gL[1], gL[2], gL[0]}, URq[3] = {gR[1], gR[2], gR[0]};
@@ -121,7 +135,7 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
                     S3[q][j] = found ? minmod3(a.alpha * sL, a.alpha * sR, S3[q][j]) : minmod2(sL, sR);
                 }
             }
-            __syncthreads();
+            cl.sync();  // the edge slopes below and the faces read slopes of other CTAs' cells
             if (tid == 0) {
                 switch (a.bound) {
                 case -2:
@@ -144,7 +158,7 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
         // interfaces
         double hs = INFINITY;
         int ab = 0, st = 0;
-        for (int j = tid; j <= m; j += NT) {
+        for (int j = gtid; j <= m; j += GNT) {
             Side1<double> L, R;
             if (a.order == 1) {
                 if (j) { L.rho = rho[j - 1]; L.u = uu[j - 1]; L.p = pp[j - 1]; }
@@ -226,12 +240,24 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
             flg[tid >> 5] = ab | (st << 1);
         }
         __syncthreads();
+        const int par = k & 1;
         if (tid == 0) {
             double v = INFINITY;
             int f = 0;
-            for (int w = 0; w < NT / 32; ++w) {
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
                 v = fmin(v, red[w]);
                 f |= flg[w];
+            }
+            part_hs[par] = v;
+            part_fl[par] = f;
+        }
+        cl.sync();  // partials of every CTA, and the faces' mid/dire/F, are now visible
+        if (tid == 0) {
+            double v = INFINITY;
+            int f = 0;
+            for (int r = 0; r < CL; ++r) {  // fmin is exact: the order of the CTAs does not matter
+                v = fmin(v, *cl.map_shared_rank(&part_hs[par], r));
+                f |= *cl.map_shared_rank(&part_fl[par], r);
             }
             sh_hs = v;
             sh_abort = f & 1;
@@ -257,7 +283,7 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
         }
         const double nu = tau / a.h;
         if (a.order == 2) {
-            for (int j = tid; j <= m; j += NT) {
+            for (int j = gtid; j <= m; j += GNT) {
                 double r = a.mid[j], u = a.mid[(m + 1) + j], p = a.mid[2 * (m + 1) + j];
                 const double dr = a.dire[j], du = a.dire[(m + 1) + j], dp = a.dire[2 * (m + 1) + j];
                 r += 0.5 * tau * dr;
@@ -275,10 +301,10 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
                 a.mid[(m + 1) + j] = u;
                 a.mid[2 * (m + 1) + j] = p;
             }
-            __syncthreads();
+            cl.sync();  // the update reads both faces of a cell, possibly computed by another CTA
         }
         int bad = 0;
-        for (int j = tid; j < m; j += NT) {
+        for (int j = gtid; j < m; j += GNT) {
             double Mom = rho[j] * uu[j] - nu * (a.F[(m + 1) + j + 1] - a.F[(m + 1) + j]);
             double Ene = rho[j] * ee[j] - nu * (a.F[2 * (m + 1) + j + 1] - a.F[2 * (m + 1) + j]);
             double r = rho[j] - nu * (a.F[j + 1] - a.F[j]);
@@ -295,6 +321,12 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
             }
         }
         bad = __syncthreads_or(bad);
+        if (tid == 0)
+            part_bad[par] = bad;
+        cl.sync();  // also publishes this step's state to every CTA
+        bad = 0;
+        for (int r = 0; r < CL; ++r)
+            bad |= *cl.map_shared_rank(&part_bad[par], r);
         if (bad)
             stop_t = 1;
         time_c += tau;
@@ -313,12 +345,23 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
         sf[tid >> 5] = nfaces;
         si[tid >> 5] = niters;
     }
+    __shared__ unsigned long long cf, ci;
     __syncthreads();
     if (tid == 0) {
         unsigned long long F = 0, I = 0;
-        for (int w = 0; w < NT / 32; ++w) {
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
             F += sf[w];
             I += si[w];
+        }
+        cf = F;
+        ci = I;
+    }
+    cl.sync();
+    if (rank == 0 && tid == 0) {
+        unsigned long long F = 0, I = 0;
+        for (int r = 0; r < CL; ++r) {
+            F += *cl.map_shared_rank(&cf, r);
+            I += *cl.map_shared_rank(&ci, r);
         }
         a.out[0] = k;
         a.out[1] = nt;
@@ -327,6 +370,50 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
         a.out[4] = halted;
         a.out[5] = (double)F;
         a.out[6] = (double)I;
+    }
+    cl.sync();  // no CTA leaves while rank 0 still reads its shared memory
+}
+
+// Launch shape of the 1D loop: one warp-multiple of threads per CTA and as
+// many CTAs (one cluster, at most 16) as give every interface its own thread,
+// so the exact solves of a step spread over up to 16 SMs.
+static cudaError_t launch_run1d(const Run1DArgs& a, cudaStream_t st)
+{
+    static int attr_set = -1;
+    if (attr_set < 0) {
+        attr_set = cudaFuncSetAttribute(k_run1d, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+        cudaGetLastError();
+    }
+    const int faces = a.m + 1;
+    int nt = 32 * ((faces + 32 * 16 - 1) / (32 * 16));
+    if (nt > 512)
+        nt = 512;
+    int cl = (faces + nt - 1) / nt;
+    if (cl > (attr_set ? 16 : 8))
+        cl = attr_set ? 16 : 8;
+    if (cl < 1)
+        cl = 1;
+    for (;;) {
+        cudaLaunchConfig_t lc;
+        memset(&lc, 0, sizeof(lc));
+        lc.gridDim = dim3(cl);
+        lc.blockDim = dim3(nt);
+        lc.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cl;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        cudaError_t e = cudaLaunchKernelEx(&lc, k_run1d, a);
+        if (e == cudaSuccess || cl == 1)
+            return e;
+        cudaGetLastError();  // a cluster this size cannot be placed: halve it
+        cl = (cl + 1) / 2;
+        nt = 32 * ((faces + 32 * cl - 1) / (32 * cl));
+        if (nt > 512)
+            nt = 512;
     }
 }
 
@@ -415,10 +502,9 @@ static int run1d(int m, int order, const double* cfg, int ncfg, double* state, c
         a.init = init; a.cur = cur; a.snaps = snaps; a.time_plot = tp; a.s = s; a.mid = mid; a.dire = dire; a.F = F;
         a.out = out;
         cudaEventRecord(e0, st);
-        k_run1d<<<1, 512, 0, st>>>(a);
+        if (!cuda_ok(launch_run1d(a, st), "1D launch")) rc = -1;
         count_launch();
         cudaEventRecord(e1, st);
-        if (!cuda_ok(cudaGetLastError(), "1D launch")) rc = -1;
     }
     double o[8] = {0};
     if (!rc && (!cuda_ok(cudaMemcpyAsync(o, out, 7 * sizeof(double), cudaMemcpyDeviceToHost, st), "1D result") ||
@@ -527,10 +613,9 @@ static int run1d_noalloc(int m, double* d_state, const double* cfg, int ncfg, in
         return -1;
     a.init = init; a.cur = d_state; a.snaps = snaps; a.time_plot = tp; a.s = s; a.mid = mid; a.dire = dire; a.F = F;
     a.out = out;
-    k_run1d<<<1, 512, 0, st>>>(a);
-    count_launch();
-    if (!cuda_ok(cudaGetLastError(), "noalloc launch"))
+    if (!cuda_ok(launch_run1d(a, st), "noalloc launch"))
         return -1;
+    count_launch();
     double o[8];
     if (!cuda_ok(cudaMemcpyAsync(o, out, 8 * sizeof(double), cudaMemcpyDeviceToHost, st), "noalloc result") ||
         !cuda_ok(cudaStreamSynchronize(st), "noalloc run"))
