@@ -209,6 +209,13 @@ static double orc_exact(double gL, double gR, double uL, double uR, double pL, d
 /* quasi-1D direct Eulerian GRP solver (2D path)                              */
 /* ------------------------------------------------------------------------- */
 
+/* Star region and wave speeds of one interface, as both direct Eulerian GRP
+ * solvers compute them (Q1D :93-134, G2D :109-153). */
+typedef struct {
+    double c_L, c_R, u_star, p_star, rho_star_L, rho_star_R, c_star_L, c_star_R, speed_L, speed_R;
+    int CRW[2];
+} orc_star;
+
 /*
  * linear_GRP_solver_Edir_Q1D, src/riemann_solver/linear_grp_solver_Edir_Q1D.c:38-554,
  * single-fluid (the volume/mass-fraction slots are constants and are dropped),
@@ -216,9 +223,12 @@ static double orc_exact(double gL, double gR, double uL, double uR, double pL, d
  * Outputs: ws = wave speeds, D = (rho,u,v,p)_t, U = (rho,u,v,p) on the t-axis,
  * S = (rho*_L, u*, rho*_R, p*).
  */
+static void orc_g2d_nonacoustic(double gL, double gR, const orc_side *Ls, const orc_side *Rs, double eps,
+                                const orc_star *st, double D[4], double U[4]);
+
 static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_side *Rs,
                           double eps, double atc, double ws[2], double D[4], double U[4], double S[4],
-                          int *newton_iters)
+                          int *newton_iters, int g2d)
 {
     const double lu = 0.0, lv = 0.0;
     const double rho_L = Ls->rho, rho_R = Rs->rho;
@@ -248,7 +258,11 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
         *newton_iters = -1;
     double c_L = sqrt(gL * p_L / rho_L);
     double c_R = sqrt(gR * p_R / rho_R);
-    double dist = sqrt((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
+    /* the genuinely-2D solver also counts the tangential velocity jump
+       (linear_grp_solver_Edir_G2D.c:112) */
+    double dist = g2d ? sqrt((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) +
+                             (v_L - v_R) * (v_L - v_R) + (p_L - p_R) * (p_L - p_R))
+                      : sqrt((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
 
     if (dist < atc && atc < 2 * eps) { /* :96-106 */
         u_star = 0.5 * (u_R + u_L);
@@ -343,6 +357,13 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
             D[2] = -(U[1] - lu) * D_v - (U[2] - lv) * T_v - T_p / U[0];
             D[3] = -(U[1] - lu) * D_p - (U[2] - lv) * T_p - U[0] * C * C * (D_u + T_v);
         }
+        return;
+    }
+
+    if (g2d) { /* the acoustic case above is the same in both solvers (G2D :156-271) */
+        orc_star st = {c_L, c_R, u_star, p_star, rho_star_L, rho_star_R, c_star_L, c_star_R,
+                       speed_L, speed_R, {CRW[0], CRW[1]}};
+        orc_g2d_nonacoustic(gL, gR, Ls, Rs, eps, &st, D, U);
         return;
     }
 
@@ -522,6 +543,265 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
     }
 }
 
+/* Q of the rarefaction-side transversal correction (G2D :367-370): the
+ * closed form has a removable singularity at gamma = 3. */
+static double orc_g2d_q(double gam, double zeta, double c_frac, double eps)
+{
+    if (gam < 3.0 - eps || gam > 3.0 + eps)
+        return (c_frac * (zeta - 1.0) + pow(c_frac, 0.5 / zeta) * zeta) / (2.0 * zeta - 1.0);
+    return 0.5 * c_frac + pow(c_frac, 0.5 / zeta) * (0.5 - 0.25 / zeta * log(c_frac));
+}
+
+/*
+ * Non-acoustic case of linear_GRP_solver_Edir_G2D,
+ * src/riemann_solver/linear_grp_solver_Edir_G2D.c:273-629, single-fluid,
+ * EXACT_TANGENT_DERIVATIVE off (the reference defines it only for its
+ * documentation build, :16-18), frame velocities lambda_u = lambda_v = 0 as
+ * GRP_2D_flux and flux_generator_x/_y leave them (flux_solver.c:163,
+ * flux_generator_x.c:35-36).  Unlike the quasi-1D solver, the tangential
+ * derivatives enter the characteristic relations of both waves (L_v, the Q
+ * term of a rarefaction, and the v T_u / v T_p corrections of d_L, d_R).
+ * c_frac is one variable across the branches, as in the reference: with two
+ * rarefactions the 3-wave's value is the one the 1-side D[2] sees (:588).
+ */
+static void orc_g2d_nonacoustic(double gL, double gR, const orc_side *Ls, const orc_side *Rs, double eps,
+                                const orc_star *st, double D[4], double U[4])
+{
+    const double lu = 0.0, lv = 0.0;
+    const double rho_L = Ls->rho, rho_R = Rs->rho;
+    const double d_rho_L = Ls->drho, d_rho_R = Rs->drho;
+    const double t_rho_L = Ls->trho, t_rho_R = Rs->trho;
+    const double u_L = Ls->u, u_R = Rs->u;
+    const double d_u_L = Ls->du, d_u_R = Rs->du;
+    const double t_u_L = Ls->tu, t_u_R = Rs->tu;
+    const double v_L = Ls->v, v_R = Rs->v;
+    const double d_v_L = Ls->dv, d_v_R = Rs->dv;
+    const double t_v_L = Ls->tv, t_v_R = Rs->tv;
+    const double p_L = Ls->p, p_R = Rs->p;
+    const double d_p_L = Ls->dp, d_p_R = Rs->dp;
+    const double t_p_L = Ls->tp, t_p_R = Rs->tp;
+    const double c_L = st->c_L, c_R = st->c_R;
+    const double u_star = st->u_star, p_star = st->p_star;
+    const double rho_star_L = st->rho_star_L, rho_star_R = st->rho_star_R;
+    const double c_star_L = st->c_star_L, c_star_R = st->c_star_R;
+    const int *CRW = st->CRW;
+    const double zetaL = (gL - 1.0) / (gL + 1.0);
+    const double zetaR = (gR - 1.0) / (gR + 1.0);
+    double C, c_frac = 1.0, TdS, d_Psi, d_Phi, VAR, Q;
+    double T_rho, T_u, T_v, T_p;
+    double H1, H2, H3, a_L, b_L, d_L, a_R, b_R, d_R, detA, L_u, L_p, L_rho, L_v;
+    double u_t_mat, p_t_mat, D0_p_tau, D0_u_tau, SmUs, SmUL, SmUR, rho_x, f;
+
+    /* trivial cases: the t-axis lies outside the wave fan (:274-304) */
+    if (st->speed_L > lu) {
+        U[0] = rho_L; U[1] = u_L; U[2] = v_L; U[3] = p_L;
+        D[0] = -(u_L - lu) * d_rho_L - (v_L - lv) * t_rho_L - rho_L * (d_u_L + t_v_L);
+        D[1] = -(u_L - lu) * d_u_L - (v_L - lv) * t_u_L - d_p_L / rho_L;
+        D[2] = -(u_L - lu) * d_v_L - (v_L - lv) * t_v_L - t_p_L / rho_L;
+        D[3] = -(u_L - lu) * d_p_L - (v_L - lv) * t_p_L - rho_L * c_L * c_L * (d_u_L + t_v_L);
+        return;
+    }
+    if (st->speed_R < lu) {
+        U[0] = rho_R; U[1] = u_R; U[2] = v_R; U[3] = p_R;
+        D[0] = -(u_R - lu) * d_rho_R - (v_R - lv) * t_rho_R - rho_R * (d_u_R + t_v_R);
+        D[1] = -(u_R - lu) * d_u_R - (v_R - lv) * t_u_R - d_p_R / rho_R;
+        D[2] = -(u_R - lu) * d_v_R - (v_R - lv) * t_v_R - t_p_R / rho_R;
+        D[3] = -(u_R - lu) * d_p_R - (v_R - lv) * t_p_R - rho_R * c_R * c_R * (d_u_R + t_v_R);
+        return;
+    }
+
+    /* tangential derivatives from the acoustic relations across the star side
+     * that holds the t-axis (:337-349, the #else branch) */
+    if (u_star < lu) {
+        T_p = 0.5 * ((t_u_L - t_u_R) * rho_star_R * c_star_R + t_p_L + t_p_R);
+        T_u = 0.5 * (t_u_L + t_u_R + (t_p_L - t_p_R) / rho_star_R / c_star_R);
+        T_rho = t_rho_R - t_p_R / (c_star_R * c_star_R) + T_p / (c_star_R * c_star_R);
+    } else {
+        T_p = 0.5 * ((t_u_L - t_u_R) * rho_star_L * c_star_L + t_p_L + t_p_R);
+        T_u = 0.5 * (t_u_L + t_u_R + (t_p_L - t_p_R) / rho_star_L / c_star_L);
+        T_rho = t_rho_L - t_p_L / (c_star_L * c_star_L) + T_p / (c_star_L * c_star_L);
+    }
+
+    if (CRW[0] && ((u_star - c_star_L) > lu)) { /* t-axis inside the 1-rarefaction (:351-384) */
+        U[1] = zetaL * (u_L + 2.0 * (c_L + lu) / (gL - 1.0));
+        C = U[1] - lu;
+        U[3] = pow(C / c_L, 2.0 * gL / (gL - 1.0)) * p_L;
+        U[0] = gL * U[3] / C / C;
+        U[2] = v_L;
+        c_frac = C / c_L;
+        TdS = (d_p_L - d_rho_L * c_L * c_L) / (gL - 1.0) / rho_L;
+        d_Psi = d_u_L + (gL * d_p_L / c_L - c_L * d_rho_L) / (gL - 1.0) / rho_L;
+        D[1] = ((1.0 + zetaL) * pow(c_frac, 0.5 / zetaL) + zetaL * pow(c_frac, (1.0 + zetaL) / zetaL));
+        D[1] = D[1] / (1.0 + 2.0 * zetaL) * TdS;
+        D[1] = D[1] - c_L * pow(c_frac, 0.5 / zetaL) * d_Psi;
+        Q = orc_g2d_q(gL, zetaL, c_frac, eps);
+        D[1] = D[1] - c_L * t_v_L * Q;
+        D[3] = U[0] * (U[1] - lu) * D[1];
+        D[0] = U[0] * (U[1] - lu) * pow(c_frac, (1.0 + zetaL) / zetaL) * TdS * (gL - 1.0);
+        D[0] = (D[0] + D[3]) / C / C - (U[2] - lv) * T_rho;
+        D[2] = -(U[1] - lu) * d_v_L * U[0] / rho_L - (U[2] - lv) * t_v_L - T_p / U[0];
+        D[2] = D[2] - (zetaL - 1.0) * (pow(c_frac, 2.0 / zetaL - 1.0) - 1.0) / (zetaL - 2.0) / U[0] * t_p_L;
+        D[3] = D[3] - (U[2] - lv) * T_p;
+        D[1] = D[1] - (U[2] - lv) * T_u + U[1] * t_v_L;
+        return;
+    }
+    if (CRW[1] && ((u_star + c_star_R) < lu)) { /* t-axis inside the 3-rarefaction (:385-418) */
+        U[1] = zetaR * (u_R - 2.0 * (c_R - lu) / (gR - 1.0));
+        C = lu - U[1];
+        U[3] = pow(C / c_R, 2.0 * gR / (gR - 1.0)) * p_R;
+        U[0] = gR * U[3] / C / C;
+        U[2] = v_R;
+        c_frac = C / c_R;
+        TdS = (d_p_R - d_rho_R * c_R * c_R) / (gR - 1.0) / rho_R;
+        d_Phi = d_u_R - (gR * d_p_R / c_R - c_R * d_rho_R) / (gR - 1.0) / rho_R;
+        D[1] = ((1.0 + zetaR) * pow(c_frac, 0.5 / zetaR) + zetaR * pow(c_frac, (1.0 + zetaR) / zetaR));
+        D[1] = D[1] / (1.0 + 2.0 * zetaR) * TdS;
+        D[1] = D[1] + c_R * pow(c_frac, 0.5 / zetaR) * d_Phi;
+        Q = orc_g2d_q(gR, zetaR, c_frac, eps);
+        D[1] = D[1] + c_R * t_v_R * Q;
+        D[3] = U[0] * (U[1] - lu) * D[1];
+        D[0] = U[0] * (U[1] - lu) * pow(c_frac, (1.0 + zetaR) / zetaR) * TdS * (gR - 1.0);
+        D[0] = (D[0] + D[3]) / C / C - (U[2] - lv) * T_rho;
+        D[2] = -(U[1] - lu) * d_v_R * U[0] / rho_R - (U[2] - lv) * t_v_R - T_p / U[0];
+        D[2] = D[2] - (zetaR - 1.0) * (pow(c_frac, 2.0 / zetaR - 1.0) - 1.0) / (zetaR - 2.0) / U[0] * t_p_R;
+        D[3] = D[3] - (U[2] - lv) * T_p;
+        D[1] = D[1] - (U[2] - lv) * T_u + U[1] * t_v_R;
+        return;
+    }
+
+    /* non-sonic case (:419-627): the t-axis is in the star region */
+    if (u_star < lu) {
+        U[0] = rho_star_R; U[1] = u_star; U[2] = v_R; U[3] = p_star;
+        C = c_star_R;
+        T_v = t_v_R;
+    } else {
+        U[0] = rho_star_L; U[1] = u_star; U[2] = v_L; U[3] = p_star;
+        C = c_star_L;
+        T_v = t_v_L;
+    }
+    /* characteristic relation across the 1-wave: a_L u_t + b_L p_t = d_L (:444-481) */
+    if (CRW[0]) {
+        a_L = 1.0;
+        b_L = 1.0 / rho_star_L / c_star_L;
+        c_frac = c_star_L / c_L;
+        TdS = (d_p_L - d_rho_L * c_L * c_L) / (gL - 1.0) / rho_L;
+        d_Psi = d_u_L + (gL * d_p_L / c_L - c_L * d_rho_L) / (gL - 1.0) / rho_L;
+        d_L = ((1.0 + zetaL) * pow(c_frac, 0.5 / zetaL) + zetaL * pow(c_frac, (1.0 + zetaL) / zetaL));
+        d_L = d_L / (1.0 + 2.0 * zetaL) * TdS;
+        d_L = d_L - c_L * pow(c_frac, 0.5 / zetaL) * d_Psi;
+        Q = orc_g2d_q(gL, zetaL, c_frac, eps);
+        d_L = d_L - c_L * t_v_L * Q;
+    } else {
+        SmUs = -sqrt(0.5 * ((gL + 1.0) * p_L + (gL - 1.0) * p_star) / rho_star_L);
+        SmUL = -sqrt(0.5 * ((gL + 1.0) * p_star + (gL - 1.0) * p_L) / rho_L);
+        VAR = sqrt((1 - zetaL) / (rho_L * (p_star + zetaL * p_L)));
+        H1 = 0.5 * VAR * (p_star + (1.0 + 2.0 * zetaL) * p_L) / (p_star + zetaL * p_L);
+        H2 = -0.5 * VAR * ((2.0 + zetaL) * p_star + zetaL * p_L) / (p_star + zetaL * p_L);
+        H3 = -0.5 * VAR * (p_star - p_L) / rho_L;
+        L_p = -1.0 / rho_L - SmUL * H2;
+        L_u = SmUL + rho_L * (c_L * c_L * H2 + H3);
+        L_rho = -SmUL * H3;
+        L_v = SmUs + rho_L * (c_L * c_L * H2 + H3);
+        a_L = 1.0 - rho_star_L * SmUs * H1;
+        b_L = -SmUs / (rho_star_L * c_star_L * c_star_L) + H1;
+        d_L = L_rho * d_rho_L + L_u * d_u_L + L_p * d_p_L + L_v * t_v_L;
+    }
+    d_L = d_L - a_L * v_L * T_u - b_L * v_L * T_p;
+    /* and across the 3-wave (:482-519) */
+    if (CRW[1]) {
+        a_R = 1.0;
+        b_R = -1.0 / rho_star_R / c_star_R;
+        c_frac = c_star_R / c_R;
+        TdS = (d_p_R - d_rho_R * c_R * c_R) / (gR - 1.0) / rho_R;
+        d_Phi = d_u_R - (gR * d_p_R / c_R - c_R * d_rho_R) / (gR - 1.0) / rho_R;
+        d_R = ((1.0 + zetaR) * pow(c_frac, 0.5 / zetaR) + zetaR * pow(c_frac, (1.0 + zetaR) / zetaR));
+        d_R = d_R / (1.0 + 2.0 * zetaR) * TdS;
+        d_R = d_R + c_R * pow(c_frac, 0.5 / zetaR) * d_Phi;
+        Q = orc_g2d_q(gR, zetaR, c_frac, eps);
+        d_R = d_R + c_R * t_v_R * Q;
+    } else {
+        SmUs = sqrt(0.5 * ((gR + 1.0) * p_R + (gR - 1.0) * p_star) / rho_star_R);
+        SmUR = sqrt(0.5 * ((gR + 1.0) * p_star + (gR - 1.0) * p_R) / rho_R);
+        VAR = sqrt((1.0 - zetaR) / (rho_R * (p_star + zetaR * p_R)));
+        H1 = 0.5 * VAR * (p_star + (1 + 2.0 * zetaR) * p_R) / (p_star + zetaR * p_R);
+        H2 = -0.5 * VAR * ((2.0 + zetaR) * p_star + zetaR * p_R) / (p_star + zetaR * p_R);
+        H3 = -0.5 * VAR * (p_star - p_R) / rho_R;
+        L_p = -1.0 / rho_R + SmUR * H2;
+        L_u = SmUR - rho_R * (c_R * c_R * H2 + H3);
+        L_rho = SmUR * H3;
+        L_v = SmUs - rho_R * (c_R * c_R * H2 + H3);
+        a_R = 1.0 + rho_star_R * SmUs * H1;
+        b_R = -(SmUs / (rho_star_R * c_star_R * c_star_R) + H1);
+        d_R = L_rho * d_rho_R + L_u * d_u_R + L_p * d_p_R + L_v * t_v_R;
+    }
+    d_R = d_R - a_R * v_R * T_u - b_R * v_R * T_p;
+    detA = a_L * b_R - b_L * a_R;
+    u_t_mat = (b_R * d_L - b_L * d_R) / detA;
+    p_t_mat = (a_L * d_R - a_R * d_L) / detA;
+    D0_p_tau = p_t_mat + U[2] * T_p;
+    D0_u_tau = u_t_mat + U[2] * T_u;
+    /* total derivatives along the t-axis (:521-530) */
+    D[1] = u_t_mat + (u_star - lu) / U[0] / C / C * D0_p_tau + (u_star - lu) * T_v;
+    D[3] = p_t_mat + (u_star - lu) * U[0] * D0_u_tau;
+    if (u_star < lu) {
+        if (CRW[1]) { /* :533-546 */
+            D[0] = rho_star_R * (u_star - lu) * pow(c_star_R / c_R, (1.0 + zetaR) / zetaR) * (d_p_R - d_rho_R * c_R * c_R) / rho_R;
+            D[0] = (D[0] + D[3] + U[2] * T_p) / c_star_R / c_star_R - (U[2] - lv) * T_rho;
+            D[2] = -U[1] * d_v_R * U[0] / rho_R - (U[2] - lv) * t_v_R - T_p / U[0];
+            D[2] = D[2] + lu * d_v_R;
+            D[2] = D[2] + u_star / c_star_R * (zetaR - 1.0) * (pow(c_frac, 2.0 / zetaR - 1.0) - 1.0) / (zetaR - 2.0) / U[0] * t_p_R;
+        } else { /* :547-577 */
+            SmUs = sqrt(0.5 * ((gR + 1.0) * p_R + (gR - 1.0) * p_star) / rho_star_R);
+            SmUR = sqrt(0.5 * ((gR + 1.0) * p_star + (gR - 1.0) * p_R) / rho_R);
+            VAR = p_R + zetaR * p_star;
+            H1 = rho_R * p_R * (1.0 - zetaR * zetaR) / VAR / VAR;
+            H2 = rho_R * p_star * (zetaR * zetaR - 1.0) / VAR / VAR;
+            H3 = (p_star + zetaR * p_R) / VAR;
+            L_rho = SmUR * H3 * d_rho_R;
+            L_u = -rho_R * (H2 * c_R * c_R + H3) * d_u_R;
+            L_p = H2 * SmUR * d_p_R;
+            L_v = -rho_R * (H2 * c_R * c_R + H3) * t_v_R;
+            D[0] = ((u_star + SmUs) / c_star_R / c_star_R - u_star * H1) * D0_p_tau + rho_star_R * u_star * SmUs * H1 * D0_u_tau;
+            D[0] = (D[0] - u_star * (L_p + L_rho + L_u + L_v)) / SmUs;
+            D[0] = D[0] - (U[2] - lv) * T_rho;
+            f = SmUR * (H2 * d_p_R + H3 * d_rho_R) - rho_R * (H2 * c_R * c_R + H3) * d_u_R;
+            rho_x = (f + H1 * (p_t_mat - rho_star_R * SmUs * u_t_mat) - D[0]) / (SmUR + u_R);
+            D[0] = D[0] + lu * rho_x;
+            D[2] = -(U[1] * (SmUR * d_v_R - t_p_R / rho_R) + (u_star + SmUs) * T_p / U[0]) / SmUs;
+            D[2] = D[2] + lu * d_v_R - (U[2] - lv) * t_v_R;
+        }
+    } else {
+        if (CRW[0]) { /* :580-593 */
+            D[0] = rho_star_L * (u_star - lu) * pow(c_star_L / c_L, (1.0 + zetaL) / zetaL) * (d_p_L - d_rho_L * c_L * c_L) / rho_L;
+            D[0] = (D[0] + D[3] + U[2] * T_p) / c_star_L / c_star_L - (U[2] - lv) * T_rho;
+            D[2] = -U[1] * d_v_L * U[0] / rho_L - (U[2] - lv) * t_v_L - T_p / U[0];
+            D[2] = D[2] + lu * d_v_L;
+            D[2] = D[2] - u_star / c_star_L * (zetaL - 1.0) * (pow(c_frac, 2.0 / zetaL - 1.0) - 1.0) / (zetaL - 2.0) / U[0] * t_p_L;
+        } else { /* :594-624 */
+            SmUs = -sqrt(0.5 * ((gL + 1.0) * p_L + (gL - 1.0) * p_star) / rho_star_L);
+            SmUL = -sqrt(0.5 * ((gL + 1.0) * p_star + (gL - 1.0) * p_L) / rho_L);
+            VAR = p_L + zetaL * p_star;
+            H1 = rho_L * p_L * (1.0 - zetaL * zetaL) / VAR / VAR;
+            H2 = rho_L * p_star * (zetaL * zetaL - 1.0) / VAR / VAR;
+            H3 = (p_star + zetaL * p_L) / VAR;
+            L_rho = SmUL * H3 * d_rho_L;
+            L_u = -rho_L * (H2 * c_L * c_L + H3) * d_u_L;
+            L_p = H2 * SmUL * d_p_L;
+            L_v = -rho_L * (H2 * c_L * c_L + H3) * t_v_L;
+            D[0] = ((u_star + SmUs) / c_star_L / c_star_L - u_star * H1) * D0_p_tau + rho_star_L * u_star * SmUs * H1 * D0_u_tau;
+            D[0] = (D[0] - u_star * (L_p + L_rho + L_u + L_v)) / SmUs;
+            D[0] = D[0] - (U[2] - lv) * T_rho;
+            f = SmUL * (H2 * d_p_L + H3 * d_rho_L) - rho_L * (H2 * c_L * c_L + H3) * d_u_L;
+            rho_x = (f + H1 * (p_t_mat - rho_star_L * SmUs * u_t_mat) - D[0]) / (SmUL + u_L);
+            D[0] = D[0] + lu * rho_x;
+            D[2] = -(U[1] * (SmUL * d_v_L - t_p_L / rho_L) + (u_star + SmUs) * T_p / U[0]) / SmUs;
+            D[2] = D[2] + lu * d_v_L - (U[2] - lv) * t_v_L;
+        }
+    }
+    D[1] = D[1] + lv * T_u;
+    D[3] = D[3] + lv * T_p;
+}
+
 static int orc_isfinite4(const double x[4])
 {
     return isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]) && isfinite(x[3]);
@@ -535,7 +815,7 @@ static int orc_isfinite4(const double x[4])
  * out[0..3] = F_rho,F_u,F_v,F_e; out[4..7] = RHO_int,U_int,V_int,P_int.
  */
 static int orc_grp2d_flux_one(double n_x, double n_y, double gamma, orc_side L, orc_side R,
-                              double tau, double eps, double out[8], int *newton_iters)
+                              double tau, double eps, double out[8], int *newton_iters, int g2d)
 {
     double u = L.u * n_x + L.v * n_y;
     double u_R = R.u * n_x + R.v * n_y;
@@ -557,7 +837,7 @@ static int orc_grp2d_flux_one(double n_x, double n_y, double gamma, orc_side L, 
     R.tu = t_u_R;
 
     double ws[2], dire[4], mid[4], star[4];
-    orc_q1d_solve(gamma, gamma, &L, &R, eps, eps, ws, dire, mid, star, newton_iters);
+    orc_q1d_solve(gamma, gamma, &L, &R, eps, eps, ws, dire, mid, star, newton_iters, g2d);
 
     int retval = 0;
     if (mid[3] < eps || mid[0] < eps)
@@ -822,6 +1102,7 @@ typedef struct {
     int m, n;
     double gamma, eps, hx, hy, alpha;
     int bx, by;
+    int g2d; /* interface solver: 0 = quasi-1D (the reference's), 1 = genuinely 2D (config[301] = 1) */
     double *snap[5][5]; /* snap[k][var]: var = rho,u,v,p,E; k < N_T */
     double *s[4], *t[4];                  /* x- and y-slopes (rho,u,v,p), [j*n+i] */
     double *F[4], *Ix[4];                 /* x-faces, [j*n+i], j = 0..m           */
@@ -1141,7 +1422,7 @@ static int orc_flux_x(orc2d *c, double *const cur[5], double tau, int transversa
             }
             int code = orc_ifvar_check2(&L, &R, c->eps) ? 1 : 0;
             double out[8];
-            if (orc_grp2d_flux_one(1.0, 0.0, c->gamma, L, R, tau, c->eps, out, NULL))
+            if (orc_grp2d_flux_one(1.0, 0.0, c->gamma, L, R, tau, c->eps, out, NULL, c->g2d))
                 code = 2;
             size_t f = AT(j, i);
             for (int k = 0; k < 4; ++k) {
@@ -1214,7 +1495,7 @@ static int orc_flux_y(orc2d *c, double *const cur[5], double tau, int transversa
             }
             int code = orc_ifvar_check2(&D, &U, c->eps) ? 1 : 0;
             double out[8];
-            if (orc_grp2d_flux_one(0.0, 1.0, c->gamma, D, U, tau, c->eps, out, NULL))
+            if (orc_grp2d_flux_one(0.0, 1.0, c->gamma, D, U, tau, c->eps, out, NULL, c->g2d))
                 code = 2;
             size_t f = ATY(j, i);
             for (int k = 0; k < 4; ++k) {
@@ -1277,6 +1558,9 @@ int orc_run_2d(int m, int n, double *rho, double *u, double *v, double *p, doubl
     memset(&c, 0, sizeof(c));
     c.m = m; c.n = n; c.gamma = gamma; c.eps = eps; c.hx = h_x; c.hy = h_y; c.alpha = cfg[41];
     c.bx = (int)cfg[17]; c.by = (int)cfg[18];
+    /* config[301] (unused by the reference) selects the genuinely-2D GRP solver
+       that flux_solver.c:189 has as its commented-out alternative */
+    c.g2d = cfg[301] == 1.0;
     const size_t mn = (size_t)m * n;
     for (k = 0; k < N_T; ++k)
         for (q = 0; q < 5; ++q)
@@ -1846,7 +2130,7 @@ void orc_grp2d_flux(int cnt, const double *in, double tau, double eps, double *o
         side_from(&L, a + 3);
         side_from(&R, a + 15);
         double o8[8];
-        int rv = orc_grp2d_flux_one(a[0], a[1], a[2], L, R, tau, eps, o8, NULL);
+        int rv = orc_grp2d_flux_one(a[0], a[1], a[2], L, R, tau, eps, o8, NULL, 0);
         double *o = out + 9 * q;
         for (int k = 0; k < 8; ++k)
             o[k] = o8[k];
@@ -1862,7 +2146,27 @@ void orc_q1d(int cnt, const double *in, double eps, double atc, double *out)
         side_from(&L, a + 1);
         side_from(&R, a + 13);
         double ws[2], D[4], U[4], S[4];
-        orc_q1d_solve(a[0], a[0], &L, &R, eps, atc, ws, D, U, S, NULL);
+        orc_q1d_solve(a[0], a[0], &L, &R, eps, atc, ws, D, U, S, NULL, 0);
+        double *o = out + 14 * q;
+        o[0] = ws[0]; o[1] = ws[1];
+        for (int k = 0; k < 4; ++k) {
+            o[2 + k] = D[k];
+            o[6 + k] = U[k];
+            o[10 + k] = S[k];
+        }
+    }
+}
+
+/* linear_GRP_solver_Edir_G2D on cnt interfaces; layout as orc_q1d. */
+void orc_g2d(int cnt, const double *in, double eps, double atc, double *out)
+{
+    for (int q = 0; q < cnt; ++q) {
+        const double *a = in + 25 * q;
+        orc_side L, R;
+        side_from(&L, a + 1);
+        side_from(&R, a + 13);
+        double ws[2], D[4], U[4], S[4];
+        orc_q1d_solve(a[0], a[0], &L, &R, eps, atc, ws, D, U, S, NULL, 1);
         double *o = out + 14 * q;
         o[0] = ws[0]; o[1] = ws[1];
         for (int k = 0; k < 4; ++k) {

@@ -26,6 +26,7 @@ void orc_riemann_exact(int cnt, const double *in, double eps, double tol, int N,
 void orc_riemann_exact_ben(int cnt, const double *in, double eps, double tol, int N, double *out);
 void orc_grp2d_flux(int cnt, const double *in, double tau, double eps, double *out);
 void orc_q1d(int cnt, const double *in, double eps, double atc, double *out);
+void orc_g2d(int cnt, const double *in, double eps, double atc, double *out);
 void orc_grp1d(int cnt, const double *in, double eps, double atc, double *out);
 
 /* Newton iteration count of the exact solver (same inputs as orc_riemann_exact);

@@ -24,6 +24,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libhydro_oracle.so")
 CRPOW_SO = os.path.join(HERE, "_build", "libhydro_oracle_crpow.so")
 REF_SO = os.path.join(HERE, "_ref", "libhydro_ref.so")
+# the reference with GRP_2D_flux calling the genuinely-2D solver (oracle/Makefile)
+REF_G2D_SO = os.path.join(HERE, "_ref", "libhydro_ref_g2d.so")
 # Where oracle/Makefile finds the reference sources (only needed to build REF_SO).
 REF_TREE = os.environ.get("HYDRO_REFERENCE", "/root/reference")
 NCONF = 400
@@ -74,13 +76,15 @@ def default_config_1d(**kw) -> np.ndarray:
 class Oracle:
     def __init__(self, which: str = "port"):
         """which: "port" (the C restatement), "crpow" (the same with a correctly
-        rounded pow) or "reference" (the reference's own sources)."""
-        path = {"port": PORT_SO, "crpow": CRPOW_SO}.get(which, REF_SO)
+        rounded pow), "reference" (the reference's own sources) or
+        "reference_g2d" (the same with GRP_2D_flux calling the genuinely-2D
+        solver; the port selects it per run with config[301] = 1)."""
+        path = {"port": PORT_SO, "crpow": CRPOW_SO, "reference_g2d": REF_G2D_SO}.get(which, REF_SO)
         if not os.path.exists(path):
             raise FileNotFoundError(f"oracle library missing: {path} (run make -C oracle)")
         self.which = which
         self.lib = ctypes.CDLL(path)
-        p = "ref_" if which == "reference" else "orc_"
+        p = "ref_" if which.startswith("reference") else "orc_"
         L = self.lib
         self._run2d = getattr(L, p + "run_2d")
         self._run2d.argtypes = [_int, _int, _dp, _dp, _dp, _dp, _dp, _dp, _int, _int, _int,
@@ -95,9 +99,11 @@ class Oracle:
         self._flux.argtypes = [_int, _dp, _dbl, _dbl, _dp]
         self._q1d = getattr(L, p + "q1d")
         self._q1d.argtypes = [_int, _dp, _dbl, _dbl, _dp]
+        self._g2d = getattr(L, p + "g2d")
+        self._g2d.argtypes = [_int, _dp, _dbl, _dbl, _dp]
         self._g1d = getattr(L, p + "grp1d")
         self._g1d.argtypes = [_int, _dp, _dbl, _dbl, _dp]
-        if which != "reference":
+        if not which.startswith("reference"):
             self._rexi = L.orc_riemann_exact_iters
             self._rexi.argtypes = [_int, _dp, _dbl, _dbl, _int, _dp]
 
@@ -164,6 +170,13 @@ class Oracle:
         inp = np.ascontiguousarray(inp, np.float64)
         out = np.zeros((len(inp), 14))
         self._q1d(len(inp), inp, eps, atc, out)
+        return out
+
+    def g2d(self, inp, eps=1e-9, atc=1e-9):
+        """linear_GRP_solver_Edir_G2D on rows laid out as for q1d."""
+        inp = np.ascontiguousarray(inp, np.float64)
+        out = np.zeros((len(inp), 14))
+        self._g2d(len(inp), inp, eps, atc, out)
         return out
 
     def grp1d(self, inp, eps=1e-9, atc=1e-9):

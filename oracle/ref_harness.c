@@ -354,6 +354,30 @@ void ref_q1d(int cnt, const double *in, double eps, double atc, double *out)
     }
 }
 
+/* linear_GRP_solver_Edir_G2D (linear_grp_solver_Edir_G2D.c:48); layout as ref_q1d. */
+void ref_g2d(int cnt, const double *in, double eps, double atc, double *out)
+{
+    for (int q = 0; q < cnt; ++q) {
+        const double *a = in + 25 * q;
+        struct i_f_var L, R;
+        memset(&L, 0, sizeof(L));
+        memset(&R, 0, sizeof(R));
+        L.gamma = R.gamma = a[0];
+        fill_side(&L, a + 1);
+        fill_side(&R, a + 13);
+        double ws[2], D[6], U[6], S[6];
+        linear_GRP_solver_Edir_G2D(ws, D, U, S, &L, &R, eps, atc);
+        double *o = out + 14 * q;
+        o[0] = ws[0];
+        o[1] = ws[1];
+        for (int k = 0; k < 4; ++k) {
+            o[2 + k] = D[k];
+            o[6 + k] = U[k];
+            o[10 + k] = S[k];
+        }
+    }
+}
+
 /* linear_GRP_solver_Edir (linear_grp_solver_Edir.c:33), 1D.
  * in: cnt x 13 = gamma, left rho,u,p,d_rho,d_u,d_p, right same.
  * out: cnt x 6 = D[0..2], U[0..2]. */

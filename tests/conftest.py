@@ -38,6 +38,19 @@ def ref():
 
 
 @pytest.fixture(scope="session")
+def ref_g2d():
+    """The reference built with GRP_2D_flux calling its genuinely-2D solver
+    (oracle/Makefile), where the reference tree exists."""
+    import oracle as orc
+
+    if not os.path.exists(orc.REF_G2D_SO):
+        if not orc.reference_available():
+            pytest.skip("reference tree not present on this machine")
+        orc.build(ref=True)
+    return orc.Oracle("reference_g2d")
+
+
+@pytest.fixture(scope="session")
 def gpu_lib():
     import torch
 

@@ -7,6 +7,11 @@ reference tree; the fixtures travel with the repository.
 
     python tests/golden/make_golden.py            # all fixtures
     python tests/golden/make_golden.py --large    # also the 1024^2 x 500 run summary
+    python tests/golden/make_golden.py --only g2d # only the genuinely-2D solver's fixtures
+
+The genuinely-2D GRP fixtures come from oracle/_ref/libhydro_ref_g2d.so, the
+same sources with GRP_2D_flux calling linear_GRP_solver_Edir_G2D (the
+alternative the reference keeps commented out at flux_solver.c:189).
 """
 from __future__ import annotations
 
@@ -87,11 +92,63 @@ RUNS_2D = [
 ]
 
 
+def g2d_inputs(rng, n):
+    """Normal-frame pairs for the genuinely-2D solver: the flux mix above plus
+    rarefaction/shock combinations on both sides of the contact (both
+    rarefactions, t-axis right of the contact, sonic points) and tangential
+    velocity jumps, which only this solver's uniform test sees."""
+    q = flux_inputs(rng, n)[:, 2:]
+    L, R = q[:, 1:13], q[:, 13:25]
+    k = n // 8
+    L[:k, 1] = -1.2; R[:k, 1] = 1.0                                  # two rarefactions, u* > 0 or < 0
+    L[k:2 * k, 1] = -0.4; R[k:2 * k, 1] = -2.0                       # shocks and rarefactions, u* < 0
+    L[2 * k:3 * k, 1] = 2.5; R[2 * k:3 * k, 1] = 0.5                 # left rarefaction sonic / shocks
+    R[3 * k:4 * k, :4] = L[3 * k:4 * k, :4]
+    R[3 * k:4 * k, 2] = L[3 * k:4 * k, 2] + 0.3                      # equal but for v: not uniform here
+    return q
+
+
+RUNS_2D_G2D = [
+    # name, m, n, kind, bx, by, steps, split, seed
+    ("fq_free", 17, 13, "fq", -4, -4, 30, 0, 7),
+    ("shear_periodic", 16, 16, "sh", -7, -7, 30, 0, 7),
+    ("fq_reflect_mixed", 20, 12, "fq", -2, -24, 30, 0, 5),
+    ("fq_split", 17, 13, "fq", -4, -4, 25, 1, 7),
+    ("shear_split", 16, 12, "sh", -7, -2, 25, 1, 2),
+]
+
+
+def make_g2d():
+    R = orc.Oracle("reference_g2d")
+    rng = np.random.default_rng(20261203)
+    qin = g2d_inputs(rng, 1024)
+    np.savez_compressed(os.path.join(HERE, "g2d.npz"), inp=qin, out=R.g2d(qin, 1e-9, 1e-9),
+                        out_acoustic=R.g2d(qin, 1e-9, np.inf))
+    runs = {}
+    for name, m, n, kind, bx, by, steps, split, seed in RUNS_2D_G2D:
+        gen = cases.four_quadrant if kind == "fq" else cases.shear_layer
+        rho, u, v, p = gen(m, n, seed)
+        cfg = orc.default_config_2d(t_all=-1, steps=steps, hx=1.0 / m, hy=1.0 / n, bx=bx, by=by, split=split)
+        cfg[301] = 1  # the port's switch for the same solver; the reference ignores config[301]
+        out = R.run_2d(rho, u, v, p, cfg, split=split)
+        for key, val in (("in_rho", rho), ("in_u", u), ("in_v", v), ("in_p", p), ("cfg", cfg)):
+            runs[f"{name}/{key}"] = val
+        for f in ("rho", "u", "v", "p", "E"):
+            runs[f"{name}/{f}"] = out[f]
+        runs[f"{name}/meta"] = np.array([out["steps"], out["time"], split])
+    np.savez_compressed(os.path.join(HERE, "runs_2d_g2d.npz"), **runs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
+    ap.add_argument("--only", choices=["all", "g2d"], default="all")
     args = ap.parse_args()
     orc.build(ref=True)
+    make_g2d()
+    if args.only == "g2d":
+        print("fixtures written to", HERE)
+        return
     R = orc.Oracle("reference")
     rng = np.random.default_rng(20241203)
 

@@ -38,6 +38,44 @@ def test_q1d_golden(port):
     assert np.array_equal(got[fin], want[fin])
 
 
+def test_g2d_golden(port):
+    """The genuinely-2D GRP solver, both atc modes, against the reference's
+    linear_GRP_solver_Edir_G2D: bit for bit, and different from the quasi-1D
+    solver on most of these rows (the cases reach its own branches)."""
+    d = load("g2d.npz")
+    assert np.array_equal(port.g2d(d["inp"], 1e-9, 1e-9), d["out"], equal_nan=True)
+    assert np.array_equal(port.g2d(d["inp"], 1e-9, np.inf), d["out_acoustic"], equal_nan=True)
+    q = port.q1d(d["inp"], 1e-9, 1e-9)
+    differ = ~np.all((q == d["out"]) | (np.isnan(q) & np.isnan(d["out"])), axis=1)
+    assert differ.mean() > 0.3
+
+
+def test_runs_2d_g2d_golden(port):
+    """Whole runs with config[301] = 1 against the reference built with
+    GRP_2D_flux calling the genuinely-2D solver (unsplit and split, every
+    boundary kind in the set)."""
+    d = load("runs_2d_g2d.npz")
+    names = _runs(d)
+    assert len(names) >= 5
+    for name in names:
+        meta = d[f"{name}/meta"]
+        cfg = d[f"{name}/cfg"]
+        assert cfg[301] == 1
+        out = port.run_2d(d[f"{name}/in_rho"], d[f"{name}/in_u"], d[f"{name}/in_v"], d[f"{name}/in_p"],
+                          cfg, split=int(meta[2]))
+        assert out["steps"] == meta[0] and out["time"] == meta[1], name
+        for f in ("rho", "u", "v", "p", "E"):
+            assert np.array_equal(out[f], d[f"{name}/{f}"]), (name, f)
+        if meta[2] == 0:
+            # the switch matters: the quasi-1D solver gives another result.  (The
+            # split sweeps pass no tangential derivatives, and without them the
+            # two solvers differ only in their uniform-pair test.)
+            q = cfg.copy()
+            q[301] = np.inf
+            other = port.run_2d(d[f"{name}/in_rho"], d[f"{name}/in_u"], d[f"{name}/in_v"], d[f"{name}/in_p"], q)
+            assert not np.array_equal(other["rho"], out["rho"]), name
+
+
 def test_grp1d_golden(port):
     d = load("grp1d.npz")
     assert np.array_equal(port.grp1d(d["inp"], 1e-9, 1e-9), d["out_grp"], equal_nan=True)
@@ -121,5 +159,26 @@ def test_port_matches_reference_random(port, ref):
     rho, u, v, p = cases.shear_layer(24, 20, 5)
     cfg = orc.default_config_2d(t_all=-1, steps=25, hx=1 / 24, hy=1 / 20, bx=-7, by=-4)
     a, b = port.run_2d(rho, u, v, p, cfg), ref.run_2d(rho, u, v, p, cfg)
+    for f in ("rho", "u", "v", "p", "E"):
+        assert np.array_equal(a[f], b[f])
+
+
+def test_g2d_port_matches_reference_random(port, ref_g2d):
+    """Fresh random faces and a fresh run against the reference's G2D build."""
+    import oracle as orc
+    from hydro_gb300 import cases
+
+    rng = np.random.default_rng(123)
+    n = 1500
+    L = np.column_stack([np.exp(rng.uniform(-3, 3, n)), rng.uniform(-3, 3, (n, 2)), np.exp(rng.uniform(-3, 3, n)),
+                         rng.normal(0, 2, (n, 8))])
+    R = np.column_stack([np.exp(rng.uniform(-3, 3, n)), rng.uniform(-3, 3, (n, 2)), np.exp(rng.uniform(-3, 3, n)),
+                         rng.normal(0, 2, (n, 8))])
+    inp = np.column_stack([np.full(n, 1.4), L, R])
+    assert np.array_equal(port.g2d(inp), ref_g2d.g2d(inp), equal_nan=True)
+    rho, u, v, p = cases.four_quadrant(22, 18, 31)
+    cfg = orc.default_config_2d(t_all=-1, steps=20, hx=1 / 22, hy=1 / 18, bx=-7, by=-2)
+    cfg[301] = 1
+    a, b = port.run_2d(rho, u, v, p, cfg), ref_g2d.run_2d(rho, u, v, p, cfg)
     for f in ("rho", "u", "v", "p", "E"):
         assert np.array_equal(a[f], b[f])
