@@ -597,6 +597,10 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
         set_error("batch: at least one step");
         return -1;
     }
+    if (ncfg > 301 && isfinite(cfg[301]) && (int)cfg[301] != HYDRO_SOLVER_Q1D) {
+        set_error("batch: built for the quasi-1D interface solver (config[301])");
+        return -1;
+    }
     const BatchShape& S = batch_shapes()[b->shape];
     int nt = 0;
     if (batch_prepare(b, cfg, ncfg, steps, stats, S, b->schedule, &nt))

@@ -159,6 +159,16 @@ static int form_from_config(const double* cfg)
     return (int)f;
 }
 
+// config[301]: the interface GRP solver (HYDRO_SOLVER_*), the quasi-1D one
+// when absent, as in the reference's GRP_2D_flux (flux_solver.c:191).
+static int solver_from_config(const double* cfg)
+{
+    double f = cfg[301];
+    if (!isfinite(f))
+        return HYDRO_SOLVER_Q1D;
+    return (int)f;
+}
+
 // The trained network shipped with the library: $HYDRO_MLP_WEIGHTS, else
 // weights/riemann_guess_6_64_64_1.f32 next to the library's build folder.
 static bool default_mlp(std::vector<float>& w, std::string& path)
@@ -183,15 +193,15 @@ static bool default_mlp(std::vector<float>& w, std::string& path)
     return got == w.size();
 }
 
-static Solver2DBase* make_solver(int m, int n, int form)
+static Solver2DBase* make_solver(int m, int n, int form, int rs)
 {
     switch (form) {
     case HYDRO_FORM_FP64:
-        return make_solver2d_f64(m, n);
+        return make_solver2d_f64(m, n, rs);
     case HYDRO_FORM_FP32:
-        return make_solver2d_f32(m, n, 0);
+        return make_solver2d_f32(m, n, 0, rs);
     case HYDRO_FORM_FP32_LEARNED: {
-        Solver2DBase* s = make_solver2d_f32(m, n, 1);
+        Solver2DBase* s = make_solver2d_f32(m, n, 1, rs);
         if (!s)
             return nullptr;
         // install the shipped network when it is there (hydro2d_set_mlp replaces it)
@@ -235,7 +245,7 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
 {
     const double t_all = config[1];
     const int form = form_from_config(config);
-    Solver2DBase* s = make_solver(m, n, form);
+    Solver2DBase* s = make_solver(m, n, form, solver_from_config(config));
     if (!s) {
         fprintf(stderr, "hydro_gb300: cannot create the 2D solver: %s\n", hydro_gb300_last_error());
         exit(5);
@@ -335,18 +345,23 @@ extern "C" {
 const char* hydro_gb300_last_error(void) { return g_err.c_str(); }
 unsigned long long hydro_gb300_kernel_launches(void) { return g_launches.load(); }
 
-int hydro2d_create(hydro2d_t** out, int m, int n, int form)
+int hydro2d_create_ex(hydro2d_t** out, int m, int n, int form, int solver)
 {
     *out = nullptr;
     if (m < 2 || n < 2) {
         set_error("grid must be at least 2 x 2");
         return -1;
     }
-    Solver2DBase* s = make_solver(m, n, form);
+    Solver2DBase* s = make_solver(m, n, form, solver);
     if (!s)
         return -1;
     *out = new hydro2d{s};
     return 0;
+}
+
+int hydro2d_create(hydro2d_t** out, int m, int n, int form)
+{
+    return hydro2d_create_ex(out, m, n, form, HYDRO_SOLVER_Q1D);
 }
 
 void hydro2d_destroy(hydro2d_t* h)

@@ -36,6 +36,7 @@ template <> struct M<double> {
     // double-double pow: agrees with a correctly rounded pow (hydro_pow.cuh)
     static __device__ __forceinline__ double pow_(double x, double y) { return dd_pow(x, y); }
     static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
+    static __device__ __forceinline__ double log_(double x) { return log(x); }
     static __device__ __forceinline__ bool finite_(double x)
     {
         return (__double_as_longlong(x) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
@@ -45,6 +46,7 @@ template <> struct M<float> {
     static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
     static __device__ __forceinline__ float pow_(float x, float y) { return exp2f(y * __log2f(x)); }
     static __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
+    static __device__ __forceinline__ float log_(float x) { return logf(x); }
     static __device__ __forceinline__ bool finite_(float x)
     {
         return (__float_as_int(x) & 0x7f800000) != 0x7f800000;
@@ -406,18 +408,29 @@ __device__ __noinline__ void q1d_star_exact(const Side<R>& L, const Side<R>& Rr,
 // uniform pairs (dist < eps) take the averaged state, all others the exact solver.
 // The uniform-pair test of q1d_star (the acoustic case), on its own: used to
 // sort faces before solving them; q1d_star makes the decision again itself.
-template <typename R>
+// RS selects the interface solver: 0 = quasi-1D (linear_grp_solver_Edir_Q1D.c:92),
+// 1 = genuinely 2D, whose distance also counts the tangential velocity jump
+// (linear_grp_solver_Edir_G2D.c:112).
+template <typename R, int RS = 0>
 __device__ __forceinline__ bool face_uniform(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G)
 {
     const R rho_L = L.rho, rho_R = Rr.rho, u_L = L.u, u_R = Rr.u, p_L = L.p, p_R = Rr.p;
-    R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
-    return StarPolicy<R>::uniform(dist, rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R), G);
+    if constexpr (RS == 1) {
+        const R v_L = L.v, v_R = Rr.v;
+        R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) +
+                             (v_L - v_R) * (v_L - v_R) + (p_L - p_R) * (p_L - p_R));
+        return StarPolicy<R>::uniform(dist, rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R) +
+                                                M<R>::abs_(v_L) + M<R>::abs_(v_R), G);
+    } else {
+        R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
+        return StarPolicy<R>::uniform(dist, rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R), G);
+    }
 }
 
 // KNOWN: 0 = make the uniform-pair decision here; 1 / 2 = the caller has
 // already made it with face_uniform (1 uniform, 2 not), so only that branch
 // is compiled into the caller.
-template <typename R, int KNOWN = 0>
+template <typename R, int KNOWN = 0, int RS = 0>
 __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
                                          StarInfo& st, R p_start = R(-1))
 {
@@ -425,7 +438,7 @@ __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, co
     S.c_L = M<R>::sqrt_(G.g * p_L / rho_L);
     S.c_R = M<R>::sqrt_(G.g * p_R / rho_R);
     if constexpr (KNOWN == 0)
-        S.acoustic = face_uniform<R>(L, Rr, G);
+        S.acoustic = face_uniform<R, RS>(L, Rr, G);
     else
         S.acoustic = (KNOWN == 1);
     if (S.acoustic) {
@@ -479,10 +492,17 @@ template <typename R>
 __device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
                                               R D[4], R U[4]);
 
+template <typename R>
+__device__ __noinline__ void g2d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G,
+                                              const Star<R>& S, R D[4], R U[4]);
+
 // Time derivatives D and t-axis values U of the quasi-1D GRP given the star
 // state: linear_grp_solver_Edir_Q1D.c:139-545 with lambda = 0.
-// KNOWN as in q1d_star (1: S is the acoustic case, 2: it is not).
-template <typename R, int KNOWN = 0>
+// KNOWN as in q1d_star (1: S is the acoustic case, 2: it is not).  RS = 1: the
+// genuinely-2D solver, whose acoustic case is this one
+// (linear_grp_solver_Edir_G2D.c:156-271) and whose non-acoustic case is
+// g2d_derivs_exact (g2d.cuh).
+template <typename R, int KNOWN = 0, int RS = 0>
 __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
                                            R D[4], R U[4])
 {
@@ -545,8 +565,12 @@ __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, 
         D[3] = -U[1] * D_p - U[2] * T_p - U[0] * C * C * (D_u + T_v);
         return;
     }
-    if constexpr (KNOWN != 1)
-        q1d_derivs_exact(L, Rr, G, S, D, U);
+    if constexpr (KNOWN != 1) {
+        if constexpr (RS == 1)
+            g2d_derivs_exact(L, Rr, G, S, D, U);
+        else
+            q1d_derivs_exact(L, Rr, G, S, D, U);
+    }
 }
 
 // Non-acoustic case of the quasi-1D GRP (:256-547), out of line like q1d_star_exact.
@@ -842,3 +866,5 @@ __device__ __forceinline__ bool ifvar_bad(const Side<R>& L, const Side<R>& Rr, R
 }
 
 }  // namespace hydro
+
+#include "g2d.cuh"

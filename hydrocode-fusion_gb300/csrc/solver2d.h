@@ -73,10 +73,11 @@ public:
     virtual int set_mlp(const float* params) = 0;
     virtual int conservation(double hx, double hy, double* out4) = 0;
     int m = 0, n = 0, form = 0;
+    int rs = 0;  // interface solver (HYDRO_SOLVER_*)
 };
 
-Solver2DBase* make_solver2d_f64(int m, int n);
-Solver2DBase* make_solver2d_f32(int m, int n, int learned);
+Solver2DBase* make_solver2d_f64(int m, int n, int rs);
+Solver2DBase* make_solver2d_f32(int m, int n, int learned, int rs);
 
 // True when HYDRO_DIRECT_HOST_ROWS=1 asks for it and the current device reads
 // and writes pageable host memory coherently (Grace-Blackwell address

@@ -4,10 +4,10 @@
 
 namespace hydro {
 
-Solver2DBase* make_solver2d_f32(int m, int n, int learned)
+Solver2DBase* make_solver2d_f32(int m, int n, int learned, int rs)
 {
     Solver2D<float>* s = new Solver2D<float>();
-    if (s->init(m, n, learned ? HYDRO_FORM_FP32_LEARNED : HYDRO_FORM_FP32)) {
+    if (s->init(m, n, learned ? HYDRO_FORM_FP32_LEARNED : HYDRO_FORM_FP32, rs)) {
         delete s;
         return nullptr;
     }

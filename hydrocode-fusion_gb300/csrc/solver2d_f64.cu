@@ -6,10 +6,10 @@
 
 namespace hydro {
 
-Solver2DBase* make_solver2d_f64(int m, int n)
+Solver2DBase* make_solver2d_f64(int m, int n, int rs)
 {
     Solver2D<double>* s = new Solver2D<double>();
-    if (s->init(m, n, HYDRO_FORM_FP64)) {
+    if (s->init(m, n, HYDRO_FORM_FP64, rs)) {
         delete s;
         return nullptr;
     }

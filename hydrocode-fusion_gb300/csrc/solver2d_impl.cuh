@@ -40,12 +40,12 @@ struct StepVariant {
     StepMaps maps[2];  // tma: descriptors of the two state buffers
 };
 
-template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false>
+template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int RS = 0>
 StepVariant<R> step_variant()
 {
     return StepVariant<R>{TJ, TI, NT, MINB,
                           LEARNED ? UnsplitSmem<R, TJ, TI>::bytes_learned : UnsplitSmem<R, TJ, TI>::bytes,
-                          (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED>, 0, 0, {}};
+                          (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED, RS>, 0, 0, {}};
 }
 
 template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int STAGES = 2>
@@ -57,28 +57,37 @@ StepVariant<R> tma_variant()
 
 // The compiled configurations, each list instantiated in its own translation
 // unit so the kernels compile in parallel (f32_gathered.cu, f32_tma.cu,
-// f32_learned.cu, f64_variants.cu).  The lists keep the configurations that
-// the autotuner picks on some workload; HYDRO_STEP_VARIANT* index into them.
+// f32_learned.cu, f64_variants.cu, g2d_f32.cu, g2d_f64.cu).  The lists keep
+// the configurations that the autotuner picks on some workload;
+// HYDRO_STEP_VARIANT* index into them.  The *_g2d lists are the unsplit step
+// with the genuinely-2D interface solver (HYDRO_SOLVER_G2D).
 void variants_f32_gathered(std::vector<StepVariant<float>>& v);
 void variants_f32_tma(std::vector<StepVariant<float>>& v);
 void variants_f32_learned(std::vector<StepVariant<float>>& v);
 void variants_f64(std::vector<StepVariant<double>>& v);
+void variants_f32_g2d(std::vector<StepVariant<float>>& v);
+void variants_f64_g2d(std::vector<StepVariant<double>>& v);
 
 template <typename R> struct Variants;
 template <> struct Variants<double> {
-    static std::vector<StepVariant<double>> all(bool)
+    static std::vector<StepVariant<double>> all(bool, int rs)
     {
         std::vector<StepVariant<double>> v;
-        variants_f64(v);
+        if (rs == HYDRO_SOLVER_G2D)
+            variants_f64_g2d(v);
+        else
+            variants_f64(v);
         return v;
     }
     static constexpr int SJ = 16, SI = 32, SNT = 256;  // split sweeps
 };
 template <> struct Variants<float> {
-    static std::vector<StepVariant<float>> all(bool learned)
+    static std::vector<StepVariant<float>> all(bool learned, int rs)
     {
         std::vector<StepVariant<float>> v;
-        if (learned) {
+        if (rs == HYDRO_SOLVER_G2D) {
+            variants_f32_g2d(v);
+        } else if (learned) {
             variants_f32_learned(v);
         } else {
             // the TMA-staged kernels first: index 0 is the default when nothing is tuned
@@ -290,6 +299,16 @@ public:
     int sms = 148;
 
     R* W(int b) { return mem + (size_t)b * 13 * plane; }
+
+    // The split scheme's sweep kernel along x (ydir 0) or y (1) for this solver's interface solver.
+    using SweepFn = void (*)(const StepArgs<R>);
+    SweepFn sweep_kernel(int ydir) const
+    {
+        using TS = Variants<R>;
+        if (rs == HYDRO_SOLVER_G2D)
+            return ydir ? k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT, 1> : k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT, 1>;
+        return ydir ? k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT, 0> : k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT, 0>;
+    }
     R* Sx(int b) { return W(b) + 5 * plane; }
     R* Ty(int b) { return W(b) + 9 * plane; }
 
@@ -324,11 +343,20 @@ public:
         return true;
     }
 
-    int init(int m_, int n_, int form_)
+    int init(int m_, int n_, int form_, int rs_)
     {
         m = m_;
         n = n_;
         form = form_;
+        rs = rs_;
+        if (rs != HYDRO_SOLVER_Q1D && rs != HYDRO_SOLVER_G2D) {
+            set_error("unknown interface solver");
+            return -1;
+        }
+        if (rs == HYDRO_SOLVER_G2D && form == HYDRO_FORM_FP32_LEARNED) {
+            set_error("the learned start is built for the quasi-1D interface solver");
+            return -1;
+        }
         ld = (n + 31) / 32 * 32;
         plane = (size_t)m * ld;
         int dev = 0;
@@ -344,7 +372,7 @@ public:
         if (!cuda_ok(cudaMalloc(&stage, sizeof(double) * 5 * (size_t)m * n), "staging")) return -1;
         if (!cuda_ok(cudaMalloc(&red, sizeof(unsigned long long)), "reduction")) return -1;
         using TS = Variants<R>;
-        variants = TS::all(form == HYDRO_FORM_FP32_LEARNED);
+        variants = TS::all(form == HYDRO_FORM_FP32_LEARNED, rs);
         if (form == HYDRO_FORM_FP32_LEARNED) {
             if (!cuda_ok(cudaMalloc(&mlp_frag, sizeof(uint32_t) * MLP_NFRAG), "network") ||
                 !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network") ||
@@ -390,11 +418,11 @@ public:
         }
         size_t smem_x = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SJ, TS::SI);
         size_t smem_y = SweepSmem<R, TS::SJ, TS::SI>::bytes(TS::SI, TS::SJ);
-        if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x), "smem attr"))
+        if (!cuda_ok(cudaFuncSetAttribute(sweep_kernel(0), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_x),
+                     "smem attr"))
             return -1;
-        if (!cuda_ok(cudaFuncSetAttribute(k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y), "smem attr"))
+        if (!cuda_ok(cudaFuncSetAttribute(sweep_kernel(1), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_y),
+                     "smem attr"))
             return -1;
         // variant override for profiling: HYDRO_STEP_VARIANT_FP64 / _FP32 / _FP32_LEARNED,
         // else HYDRO_STEP_VARIANT for every form
@@ -739,12 +767,12 @@ public:
             } else if (r.dir == 1) {
                 a.src_s = Sx(s); a.dst_s = Sx(s ^ 1);
                 a.src_t = Ty(t); a.dst_t = Ty(t);
-                k_sweep<R, 0, TS::SJ, TS::SI, TS::SNT><<<gs, TS::SNT, smem_x, stream>>>(a);
+                sweep_kernel(0)<<<gs, TS::SNT, smem_x, stream>>>(a);
                 s ^= 1;
             } else {
                 a.src_s = Sx(s); a.dst_s = Sx(s);
                 a.src_t = Ty(t); a.dst_t = Ty(t ^ 1);
-                k_sweep<R, 1, TS::SJ, TS::SI, TS::SNT><<<gs, TS::SNT, smem_y, stream>>>(a);
+                sweep_kernel(1)<<<gs, TS::SNT, smem_y, stream>>>(a);
                 t ^= 1;
             }
             count_launch();

@@ -218,6 +218,7 @@ __device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigne
 // (FP32-reconstructed) sides; returns the face's error code (0, 1 or 2) as
 // the FP64 solve sees it.  Out of line and called from a separate pass after
 // the face passes: it runs on a handful of faces per run.
+template <int RS>
 static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, const Side<float>& Rr, double g,
                                                          double eps, double tau, bool ydir, FaceOut<float>& o)
 {
@@ -233,9 +234,9 @@ static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, c
     Star<double> S;
     StarInfo st;
     st.fallback = 0;
-    q1d_star<double, 0>(Ld, Rd, G, S, st, -1.0);
+    q1d_star<double, 0, RS>(Ld, Rd, G, S, st, -1.0);
     double D[4], U[4];
-    q1d_derivs(Ld, Rd, G, S, D, U);
+    q1d_derivs<double, 0, RS>(Ld, Rd, G, S, D, U);
     const int bad = star_dire_check2(U, D, eps) ? 2 : (ifvar_bad(Ld, Rd, eps) ? 1 : 0);
     FaceOut<double> od;
     face_flux<double>(D, U, tau, 0.5 * tau, G, od, ydir);
@@ -248,8 +249,9 @@ static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, c
 }
 
 // Solve one face given its two sides in the face's normal frame (KNOWN as in
-// q1d_star: whether the uniform-pair decision has already been made).
-template <typename R, int KNOWN = 0>
+// q1d_star: whether the uniform-pair decision has already been made; RS: the
+// interface solver, 0 = quasi-1D, 1 = genuinely 2D).
+template <typename R, int KNOWN = 0, int RS = 0>
 __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, R tau, R htau,
                                           FaceOut<R>& o, int& iters, int& fallback, bool ydir, R p_start = R(-1))
 {
@@ -257,9 +259,9 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
     Star<R> S;
     StarInfo st;
     st.fallback = 0;
-    q1d_star<R, KNOWN>(L, Rr, G, S, st, p_start);
+    q1d_star<R, KNOWN, RS>(L, Rr, G, S, st, p_start);
     R D[4], U[4];
-    q1d_derivs<R, KNOWN>(L, Rr, G, S, D, U);
+    q1d_derivs<R, KNOWN, RS>(L, Rr, G, S, D, U);
     iters = st.iters;
     fallback = st.fallback;
     if (star_dire_check2(U, D, G.eps))
@@ -356,13 +358,14 @@ struct StageLayout {
 //     J0-2.., columns I0-X.., pitch BW) at W and the 8 previous-slope planes
 //     (rows J0-1.., same columns) at B; only the ghost cells of tiles at the
 //     domain edge are gathered.  FX may alias B (B is dead after phase 2).
-template <typename R, int TJ, int TI, int NT, bool LEARNED, bool STAGED>
+template <typename R, int TJ, int TI, int NT, bool LEARNED, bool STAGED, int RS = 0>
 __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
                                           R* __restrict__ W,
                                           const R* B, R* __restrict__ S, R* FX, R* __restrict__ FY,
                                           unsigned short* __restrict__ Q, float* __restrict__ P,
                                           const MlpShared& Mlp)
 {
+    static_assert(!(LEARNED && RS != 0), "the learned start is built for the quasi-1D interface solver");
     using SM = UnsplitSmem<R, TJ, TI>;
     using SL = StageLayout<R, TJ, TI>;
     const int tid = threadIdx.x;
@@ -563,7 +566,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         const bool ydir = f >= NFX;
         FaceOut<R> o;
         int it, fbk;
-        int code = solve_face<R, decltype(known)::value>(L, Rr, G, a.tau, a.htau, o, it, fbk, ydir, p_start);
+        int code = solve_face<R, decltype(known)::value, RS>(L, Rr, G, a.tau, a.htau, o, it, fbk, ydir, p_start);
         if (it >= 0) {
             my_newton++;
             my_iters += it;
@@ -599,7 +602,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         Side<R> L, Rr;
         int lj = 0, li = 0, j = 0, i = 0;
         const bool active = f < NF && sides(f, L, Rr, lj, li, j, i);
-        const bool uni = active && face_uniform<R>(L, Rr, G);
+        const bool uni = active && face_uniform<R, RS>(L, Rr, G);
         const bool need = active && !uni;
         const unsigned want = __ballot_sync(0xffffffffu, need);
         if (want) {
@@ -669,7 +672,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                 sides(f, L, Rr, lj, li, j, i);
                 FaceOut<R> o;
                 const bool ydir = f >= NFX;
-                const int code = solve_face_fp64_retry(L, Rr, G.g64, G.eps64, (double)a.tau, ydir, o);
+                const int code = solve_face_fp64_retry<RS>(L, Rr, G.g64, G.eps64, (double)a.tau, ydir, o);
                 if (!ydir) {
                     report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
 #pragma unroll
@@ -738,7 +741,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
 }
 
 // The gathered tile with its shared-memory carve-up (W | S | FX | FY).
-template <typename R, int TJ, int TI, int NT, bool LEARNED>
+template <typename R, int TJ, int TI, int NT, bool LEARNED, int RS = 0>
 __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
                                              unsigned char* smem_raw, const MlpShared& Mlp)
 {
@@ -749,10 +752,10 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const Gas<R>&
     R* FY = FX + SM::nFX;
     unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + SM::bytes_f);
     float* P = LEARNED ? reinterpret_cast<float*>(smem_raw + SM::p_off) : nullptr;
-    tile_body<R, TJ, TI, NT, LEARNED, false>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, P, Mlp);
+    tile_body<R, TJ, TI, NT, LEARNED, false, RS>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, P, Mlp);
 }
 
-template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false>
+template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false, int RS = 0>
 __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
 {
     using SM = UnsplitSmem<R, TJ, TI>;
@@ -762,7 +765,7 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
     MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + SM::mlp_off);
     if (LEARNED)
         mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
-    unsplit_tile<R, TJ, TI, NT, LEARNED>(a, a.G, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
+    unsplit_tile<R, TJ, TI, NT, LEARNED, RS>(a, a.G, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
 }
 
 // ---------------------------------------------------------------------------
@@ -901,7 +904,7 @@ struct SweepSmem {
     }
 };
 
-template <typename R, int YDIR, int TJ, int TI, int NT>
+template <typename R, int YDIR, int TJ, int TI, int NT, int RS = 0>
 __global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R> a)
 {
     if (halt_prologue(a.ctl, a.seq))
@@ -1002,7 +1005,7 @@ __global__ void __launch_bounds__(NT) k_sweep(const __grid_constant__ StepArgs<R
         FaceOut<R> o;
         int it;
         int fbk;
-        const int code = solve_face<R>(L, Rr, a.G, a.tau, a.htau, o, it, fbk, YDIR != 0);
+        const int code = solve_face<R, 0, RS>(L, Rr, a.G, a.tau, a.htau, o, it, fbk, YDIR != 0);
         if (it >= 0) {
             my_newton++;
             my_iters += it;

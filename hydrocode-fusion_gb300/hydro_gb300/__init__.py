@@ -21,6 +21,9 @@ NCONF = 400
 FORM_FP64 = 0
 FORM_FP32 = 1
 FORM_FP32_LEARNED = 2
+# interface GRP solver of the 2D schemes (config[301], HYDRO_SOLVER_*)
+SOLVER_Q1D = 0
+SOLVER_G2D = 1
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _fp = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
@@ -89,6 +92,9 @@ def lib() -> ctypes.CDLL:
     L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
     L.hydro2d_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.hydro2d_create.restype = ctypes.c_int
+    L.hydro2d_create_ex.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int]
+    L.hydro2d_create_ex.restype = ctypes.c_int
     L.hydro2d_destroy.argtypes = [ctypes.c_void_p]
     L.hydro2d_destroy.restype = None
     L.hydro2d_upload.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.c_void_p, ctypes.c_double]
@@ -151,7 +157,7 @@ def config_2d(**kw) -> np.ndarray:
     c[110] = 0.72; c[210] = 0.0; c[211] = 0.0; c[212] = 0.0
     c[4] = 1e-9; c[6] = 1.4; c[7] = 0.45
     names = {"t_all": 1, "eps": 4, "steps": 5, "gamma": 6, "cfl": 7, "hx": 10, "hy": 11,
-             "tau": 16, "bx": 17, "by": 18, "split": 33, "alpha": 41, "form": 300}
+             "tau": 16, "bx": 17, "by": 18, "split": 33, "alpha": 41, "form": 300, "solver": 301}
     for k, v in kw.items():
         c[names[k]] = v
     if not (math.isfinite(c[1]) and c[1] >= 0.0):
@@ -174,10 +180,10 @@ class Solver2D:
     Arrays are x-major numpy arrays of shape (m, n): value of cell (x=j, y=i) at [j, i].
     """
 
-    def __init__(self, m: int, n: int, form: int = FORM_FP64):
-        self.m, self.n, self.form = m, n, form
+    def __init__(self, m: int, n: int, form: int = FORM_FP64, solver: int = SOLVER_Q1D):
+        self.m, self.n, self.form, self.solver = m, n, form, solver
         h = ctypes.c_void_p()
-        if lib().hydro2d_create(ctypes.byref(h), m, n, form) != 0:
+        if lib().hydro2d_create_ex(ctypes.byref(h), m, n, form, solver) != 0:
             raise RuntimeError("hydro2d_create failed: " + last_error())
         self._h = h
 
@@ -252,11 +258,12 @@ class Solver2D:
         return info
 
 
-def run_2d(rho, u, v, p, cfg, split=False, form=FORM_FP64, stats=False, mlp=None):
+def run_2d(rho, u, v, p, cfg, split=False, form=FORM_FP64, stats=False, mlp=None, solver=SOLVER_Q1D):
     """Upload, run, download; returns (state dict, RunInfo).  The learned form
-    uses `mlp` (a parameter vector) or the shipped trained weights."""
+    uses `mlp` (a parameter vector) or the shipped trained weights; `solver`
+    picks the interface GRP solver (SOLVER_Q1D or SOLVER_G2D)."""
     m, n = np.shape(rho)
-    s = Solver2D(m, n, form)
+    s = Solver2D(m, n, form, solver)
     try:
         if form == FORM_FP32_LEARNED:
             s.set_mlp(load_weights() if mlp is None else mlp)

@@ -32,7 +32,9 @@ extern "C" {
  * defined in src/hydrocode_2D/hydrocode.c:123 and src/hydrocode_1D/hydrocode.c:111).
  * Indices follow the reference's doc/config.csv; this library additionally reads
  *   config[300]  precision/guess form of the 2D scheme (HYDRO_FORM_*; INFINITY or
- *                absent = HYDRO_FORM_FP64, the reference's arithmetic). */
+ *                absent = HYDRO_FORM_FP64, the reference's arithmetic);
+ *   config[301]  interface GRP solver of the 2D schemes (HYDRO_SOLVER_*; INFINITY or
+ *                absent = HYDRO_SOLVER_Q1D, the one the reference calls). */
 extern double config[];
 
 /* Same member order as the reference's struct cell_var_stru
@@ -81,6 +83,13 @@ enum {
     HYDRO_FORM_FP32_LEARNED = 2  /* FP32 form with the learned Newton starting pressure */
 };
 
+/* Interface GRP solver of GRP_2D_flux (src/flux_calc/flux_solver.c:187-193). */
+enum {
+    HYDRO_SOLVER_Q1D = 0,  /* linear_GRP_solver_Edir_Q1D (flux_solver.c:191), the reference's call */
+    HYDRO_SOLVER_G2D = 1   /* linear_GRP_solver_Edir_G2D with atc = eps, the alternative the
+                              reference keeps commented out at flux_solver.c:189 */
+};
+
 typedef struct hydro2d hydro2d_t;
 
 /* Outcome of a run, in the reference's terms. */
@@ -100,6 +109,10 @@ typedef struct {
 
 /* Create a solver for an m (x) by n (y) grid in the given form. 0 on success. */
 int hydro2d_create(hydro2d_t **out, int m, int n, int form);
+/* The same with the interface solver chosen (HYDRO_SOLVER_*; hydro2d_create uses
+ * HYDRO_SOLVER_Q1D).  HYDRO_SOLVER_G2D is available in HYDRO_FORM_FP64 and
+ * HYDRO_FORM_FP32; the learned form is built for the quasi-1D solver (-1). */
+int hydro2d_create_ex(hydro2d_t **out, int m, int n, int form, int solver);
 void hydro2d_destroy(hydro2d_t *h);
 /* Upload an x-major (value of cell (j,i) at [j*n+i]) FP64 state; E may be NULL,
  * then E = 0.5 u^2 + p/(gamma-1)/rho + 0.5 v^2 as the reference's driver computes it. */
