@@ -146,14 +146,15 @@ def rel_l1(a, b):
     return float(np.abs(a - b).sum() / d) if d > 0 else float(np.abs(a - b).sum())
 
 
-def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dist=None, bnd=-4):
+def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dist=None, bnd=-4, solver=0):
     """Tune, warm up, then time K steps of one form from the initial state
-    (boundary code bnd on all sides).  Returns a dict with the rate, the final
-    state and statistics."""
+    (boundary code bnd on all sides; solver = the interface GRP solver,
+    config[301]).  Returns a dict with the rate, the final state and
+    statistics."""
     rho, u, v, p = state
-    cfgK = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd)
-    cfgW = hg.config_2d(t_all=-1, steps=W, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd)
-    s = hg.Solver2D(m, n, form)
+    cfgK = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd, solver=solver)
+    cfgW = hg.config_2d(t_all=-1, steps=W, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd, solver=solver)
+    s = hg.Solver2D(m, n, form, solver)
     res = {}
     try:
         if form == hg.FORM_FP32_LEARNED:
@@ -195,7 +196,8 @@ def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dis
         res["state"] = s.download()
         if stats_steps > 0:
             s.upload(rho, u, v, p)
-            i2 = s.run(hg.config_2d(t_all=-1, steps=stats_steps, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd), stats=True)
+            i2 = s.run(hg.config_2d(t_all=-1, steps=stats_steps, hx=1.0 / m, hy=1.0 / n, bx=bnd, by=bnd,
+                                    solver=solver), stats=True)
             faces = 2.0 * m * n * stats_steps
             res["newton"] = {"steps": stats_steps, "exact_solves_per_face": i2.newton_faces / faces,
                              "iters_per_exact_solve": (i2.newton_iters / i2.newton_faces) if i2.newton_faces else 0.0,
@@ -302,6 +304,24 @@ def shear_suite(hg, m, n, K, W, tune, stats_steps):
     return out
 
 
+def g2d_suite(hg, state, m, n, K, K64, W, tune, stats_steps):
+    """The same four-quadrant workload with the genuinely-2D interface solver
+    (config[301] = 1, the alternative GRP_2D_flux keeps commented out): FP32
+    and FP64 forms timed, FP32 compared with FP64."""
+    res = {}
+    for key, form, steps in (("fp32", hg.FORM_FP32, K), ("fp64", hg.FORM_FP64, K64)):
+        if steps > 0:
+            res[key] = timed_form(hg, form, state, m, n, steps, W, tune, stats_steps, solver=hg.SOLVER_G2D)
+    out = {"workload": workload_name(m, n) + ", genuinely-2D GRP interface solver (config[301] = 1)"}
+    for key, r in res.items():
+        out[key] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "steps": r["steps_done"],
+                    "kernel_variant": r["kernel_variant"], "newton": r.get("newton"), "halted": r["halted"]}
+    if "fp64" in res and res["fp64"]["steps_done"] == res["fp32"]["steps_done"]:
+        out["fp32"]["l1_vs_fp64"] = {f: rel_l1(res["fp32"]["state"][f], res["fp64"]["state"][f])
+                                     for f in ("rho", "u", "v", "p")}
+    return out
+
+
 def reference_arm(args, m, n, rank):
     if rank != 0:
         return
@@ -337,6 +357,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-shear", action="store_true")
+    ap.add_argument("--no-g2d", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=300)
     args = ap.parse_args()
@@ -410,6 +431,7 @@ def main():
     e2e = None if args.no_e2e else e2e_run(hg, state, m, n, K)
     batch = None if args.no_batch else batch_run(hg, args.batch_count, args.batch_steps, 5, 8)
     shear = None if args.no_shear else shear_suite(hg, m, n, K, W, tune, args.stats_steps)
+    g2d = None if args.no_g2d else g2d_suite(hg, state, m, n, K, k64, W, tune, args.stats_steps)
 
     cpu = None
     if not args.no_cpu:
@@ -425,7 +447,7 @@ def main():
                        "grid": [m, n], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "no flush: 13 planes x 4 B x 16.8M cells = 872 MB per state >> 129 MB L2"},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "gpu_launches": int(head["launches"]),
-            "clocks": head["clocks"], "forms": forms, "shear": shear, "batch": batch}
+            "clocks": head["clocks"], "forms": forms, "shear": shear, "g2d": g2d, "batch": batch}
     print(json.dumps(line), flush=True)
 
 

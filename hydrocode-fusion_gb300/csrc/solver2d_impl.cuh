@@ -48,11 +48,11 @@ StepVariant<R> step_variant()
                           (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED, RS>, 0, 0, {}};
 }
 
-template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int STAGES = 2>
+template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int STAGES = 2, int RS = 0>
 StepVariant<R> tma_variant()
 {
     return StepVariant<R>{TJ, TI, NT, MINB, TmaSmem<R, TJ, TI, LEARNED, STAGES>::launch_bytes,
-                          (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED, STAGES>, STAGES, 0, {}};
+                          (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED, STAGES, RS>, STAGES, 0, {}};
 }
 
 // The compiled configurations, each list instantiated in its own translation

@@ -801,7 +801,7 @@ struct TmaSmem {
 
 constexpr unsigned long long TMA_WAIT_NS = 2000000000ull;  // 2 s
 
-template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false, int STAGES = 2>
+template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false, int STAGES = 2, int RS = 0>
 __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ StepArgs<R> a,
                                                        const __grid_constant__ StepMaps maps)
 {
@@ -874,7 +874,8 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
         unsigned char* cur = smem_raw + stg * SL::bytes;
         R* W = reinterpret_cast<R*>(cur + SL::a_off);
         R* B = reinterpret_cast<R*>(cur + SL::b_off);
-        tile_body<R, TJ, TI, NT, LEARNED, true>(a, a.G, (t % nti) * TI, (t / nti) * TJ, W, B, S, B, FY, Q, P, Mlp);
+        tile_body<R, TJ, TI, NT, LEARNED, true, RS>(a, a.G, (t % nti) * TI, (t / nti) * TJ, W, B, S, B, FY, Q, P,
+                                                    Mlp);
     }
     if (failed && threadIdx.x == 0) {
         // let the copies still in flight land (bounded) before the CTA exits, then report
