@@ -15,6 +15,7 @@
 #include <sys/types.h>
 #include <unistd.h>
 
+#include "hydro_fastio.h"
 #include "hydro_io.h"
 
 #define PATH_LEN (FILENAME_MAX + 40)
@@ -395,23 +396,59 @@ void config_write(const char *add_out, const double *cpu_time, const char *name)
     fclose(fp);
 }
 
-static FILE *open_input(const char *add_in, const char *var, char *add, int must)
+/* Initial data file of one variable: <var>.txt, else <var>.dat (as the
+ * reference, file_1D_in.c:104-110), else <var>.bin (the binary FP64 format of
+ * hydro_fastio.h).  Returns 1 text, 2 binary, 0 none (after the reference's
+ * message). */
+static int find_input(const char *add_in, const char *var, char *add)
 {
-    FILE *fp;
-    snprintf(add, PATH_LEN, "%s%s.txt", add_in, var);
-    if ((fp = fopen(add, "r")) == NULL) {
-        snprintf(add, PATH_LEN, "%s%s.dat", add_in, var);
-        fp = fopen(add, "r");
+    static const char *ext[3] = {"txt", "dat", "bin"};
+    for (int e = 0; e < 3; ++e) {
+        snprintf(add, PATH_LEN, "%s%s.%s", add_in, var, ext[e]);
+        if (access(add, R_OK) == 0)
+            return e < 2 ? 1 : 2;
     }
-    if (!fp) {
-        printf("Cannot open initial data file: %s!\n", var);
-        if (must)
-            exit(1);
-    }
-    return fp;
+    printf("Cannot open initial data file: %s!\n", var);
+    return 0;
 }
 
-/* 1D initial data (src/file_io/file_1D_in.c:93-151). */
+/* Numbers of one initial data file: *lines x *columns (2D text: lines are y
+ * rows; binary: n_y x n_x of its first plane).  Exits as the reference's
+ * initialisation does on a read error (2 data, 5 memory). */
+static double *read_input(const char *add, int kind, int check_columns, int *lines, int *columns, long long *num)
+{
+    double *d = NULL;
+    if (kind == 2) {
+        int ndim, n_x, n_y, nsnap;
+        double *times = NULL;
+        int rc = hio_bin_read(add, &ndim, &n_x, &n_y, &nsnap, &times, &d);
+        free(times);
+        if (rc) {
+            printf("Error in reading the binary initial data file '%s'!\n", add);
+            exit(rc == 5 ? 5 : 2);
+        }
+        *lines = n_y;
+        *columns = n_x;
+        *num = (long long)n_x * n_y;  /* the first plane */
+        return d;
+    }
+    int rc = hio_read_table(add, check_columns, lines, columns, num, &d);
+    if (rc == 5) {
+        printf("NOT enough memory! %s\n", add);
+        exit(5);
+    }
+    if (rc == 3)  /* an entry strtod does not take: the reference's flu_var_read failure */
+        exit(2);
+    if (rc || *num < 1) {
+        printf("Error in counting fluid variables in initial data file: %s!\n", add);
+        exit(2);
+    }
+    return d;
+}
+
+/* 1D initial data (src/file_io/file_1D_in.c:93-151); the numbers are read by
+ * hio_read_table (several threads, the same values as the reference's getc
+ * reader). */
 struct flu_var initialize_1D(const char *name, int *N, int *N_plot, double *time_plot[])
 {
     struct flu_var FV0 = {NULL, NULL, NULL, NULL};
@@ -422,29 +459,18 @@ struct flu_var initialize_1D(const char *name, int *N, int *N_plot, double *time
     const char *vars[3] = {"RHO", "U", "P"};
     double **dst[3] = {&FV0.RHO, &FV0.U, &FV0.P};
     for (int q = 0; q < 3; ++q) {
-        FILE *fp = open_input(add_in, vars[q], add, 1);
-        int num = flu_var_count(fp, add);
-        if (num < 1) {
-            printf("Error in counting fluid variables in initial data file: %s!\n", vars[q]);
-            fclose(fp);
-            exit(2);
-        }
+        int kind = find_input(add_in, vars[q], add);
+        if (!kind)
+            exit(1);
+        int lines, columns;
+        long long num;
+        *dst[q] = read_input(add, kind, 0, &lines, &columns, &num);
         if (isinf(config[3]))
             config[3] = (double)num;
-        else if (num != (int)config[3]) {
-            printf("Input unequal! num_%s=%d, num_cell=%d.\n", vars[q], num, (int)config[3]);
+        else if (num != (long long)config[3]) {
+            printf("Input unequal! num_%s=%lld, num_cell=%d.\n", vars[q], num, (int)config[3]);
             exit(2);
         }
-        *dst[q] = (double *)malloc(num * sizeof(double));
-        if (!*dst[q]) {
-            printf("NOT enough memory! %s\n", vars[q]);
-            exit(5);
-        }
-        if (flu_var_read(fp, *dst[q], num)) {
-            fclose(fp);
-            exit(2);
-        }
-        fclose(fp);
     }
     printf("'%s' data initialized, grid cell number = %d.\n", add_in, (int)config[3]);
     return FV0;
@@ -462,34 +488,22 @@ struct flu_var initialize_2D(const char *name, int *N, int *N_plot, double *time
     const char *vars[4] = {"RHO", "U", "V", "P"};
     double **dst[4] = {&FV0.RHO, &FV0.U, &FV0.V, &FV0.P};
     for (int q = 0; q < 4; ++q) {
-        FILE *fp = open_input(add_in, vars[q], add, 1);
-        int column = 0, line = flu_var_count_line(fp, add, &column);
-        int num = line * column;
-        if (num < 1) {
-            printf("Error in counting fluid variables in initial data file! %s\n", add);
-            fclose(fp);
-            exit(2);
-        }
+        int kind = find_input(add_in, vars[q], add);
+        if (!kind)
+            exit(1);
+        int line, column;
+        long long num;
+        *dst[q] = read_input(add, kind, 1, &line, &column, &num);
         if (isinf(config[3]))
             config[3] = (double)num;
         if (isinf(config[13]))
             config[13] = (double)column;
         if (isinf(config[14]))
             config[14] = (double)line;
-        else if (num != (int)config[3] || column != (int)config[13] || line != (int)config[14]) {
+        else if (num != (long long)config[3] || column != (int)config[13] || line != (int)config[14]) {
             printf("Input unequal! %s\n", add);
             exit(2);
         }
-        *dst[q] = (double *)malloc(num * sizeof(double));
-        if (!*dst[q]) {
-            printf("NOT enough memory! %s\n", add);
-            exit(5);
-        }
-        if (flu_var_read(fp, *dst[q], num)) {
-            fclose(fp);
-            exit(2);
-        }
-        fclose(fp);
     }
     printf("'%s' data initialized, line = %d, column = %d.\n", add_in, (int)config[14], (int)config[13]);
     return FV0;
@@ -515,36 +529,93 @@ static void write_time_plot(const char *add_out, const int N, const double time_
     fclose(fp);
 }
 
-/* 1D .dat output: one line per stored time (src/file_io/file_1D_out.c:49-95). */
+/* Output formats, config[302] (unused by the reference): 0 or absent = the
+ * reference's %.10g text, 1 = text and binary (<var>.bin, hydro_fastio.h),
+ * 2 = binary only. */
+static int out_text(void) { return !(isfinite(config[302]) && (int)config[302] == 2); }
+static int out_bin(void) { return isfinite(config[302]) && ((int)config[302] == 1 || (int)config[302] == 2); }
+
+/* value accessors of the writers: one row of a plane per call site */
+typedef struct {
+    double **a;       /* 2D: a[j][i] = x-major cell array; 1D: a[k][j] */
+    double **X, **Y;  /* 2D node coordinates */
+    int q, k;
+} out_ctx;
+
+static double val_1d(const void *ctx, int r, int c)
+{
+    const out_ctx *o = (const out_ctx *)ctx;
+    return o->a[o->k + r][c];
+}
+static double val_1d_x(const void *ctx, int r, int c)
+{
+    const out_ctx *o = (const out_ctx *)ctx;
+    return 0.5 * (o->X[o->k + r][c] + o->X[o->k + r][c + 1]);
+}
+static double val_2d(const void *ctx, int r, int c)
+{
+    const out_ctx *o = (const out_ctx *)ctx;
+    return o->a[c][r];  /* row r = y index i, column c = x index j */
+}
+static double val_2d_center(const void *ctx, int r, int c)
+{
+    const out_ctx *o = (const out_ctx *)ctx;
+    double **Z = o->q == 5 ? o->X : o->Y;
+    return 0.25 * (Z[c][r] + Z[c][r + 1] + Z[c + 1][r] + Z[c + 1][r + 1]);
+}
+
+/* 1D binary output: N snapshots of one row of m values. */
+static void write_bin_1d(const char *add_out, const char *var, int m, int N, const double time_plot[], out_ctx *o,
+                         hio_value_fn f)
+{
+    char file[PATH_LEN + 64];
+    snprintf(file, sizeof(file), "%s%s.bin", add_out, var);
+    FILE *fp = hio_bin_create(file, 1, m, 1, N, time_plot);
+    if (!fp) {
+        printf("Cannot open solution output file: %s!\n", var);
+        exit(1);
+    }
+    int rc = 0;
+    for (int k = 0; k < N && !rc; ++k) {
+        o->k = k;
+        rc = hio_bin_plane(fp, 1, m, f, o);
+    }
+    if (fclose(fp) != 0 || rc) {
+        printf("Error in writing solution output file: %s!\n", var);
+        exit(1);
+    }
+}
+
+/* 1D .dat output: one line per stored time (src/file_io/file_1D_out.c:49-95);
+ * the lines are formatted by several threads (the same bytes). */
 void file_1D_write(const int m, const int N, const struct cell_var_stru CV, double *X[], const double *cpu_time,
                    const char *problem, const double time_plot[])
 {
     char add_out[PATH_LEN];
     example_io(problem, add_out, 0);
     double **vars[4] = {CV.RHO, CV.U, CV.P, CV.E};
-    const char *names[4] = {"RHO", "U", "P", "E"};
-    for (int q = 0; q < 4; ++q) {
-        FILE *fp = open_output(add_out, names[q]);
-        for (int k = 0; k < N; ++k) {
-            for (int j = 0; j < m; ++j)
-                fprintf(fp, "%.10g\t", vars[q][k][j]);
-            fprintf(fp, "\n");
+    const char *names[5] = {"RHO", "U", "P", "E", "X"};
+    for (int q = 0; q < 5; ++q) {
+        out_ctx o = {q < 4 ? vars[q] : NULL, X, NULL, q, 0};
+        hio_value_fn f = q < 4 ? val_1d : val_1d_x;
+        if (out_text()) {
+            FILE *fp = open_output(add_out, names[q]);
+            if (hio_write_text(fp, N, m, f, &o)) {
+                printf("Error in writing solution output file: %s!\n", names[q]);
+                exit(1);
+            }
+            fclose(fp);
         }
-        fclose(fp);
+        if (out_bin())
+            write_bin_1d(add_out, names[q], m, N, time_plot, &o, f);
     }
-    FILE *fp = open_output(add_out, "X");
-    for (int k = 0; k < N; ++k) {
-        for (int j = 0; j < m; ++j)
-            fprintf(fp, "%.10g\t", 0.5 * (X[k][j] + X[k][j + 1]));
-        fprintf(fp, "\n");
-    }
-    fclose(fp);
     write_time_plot(add_out, N, time_plot);
     config_write(add_out, cpu_time, problem);
 }
 
 /* 2D .dat output: per stored time, one line per y row, blank lines between
- * times (src/file_io/file_2D_out.c:55-101). */
+ * times (src/file_io/file_2D_out.c:55-101); rows formatted by several threads
+ * (the same bytes). */
 void file_2D_write(const int n_x, const int n_y, const int N, const struct cell_var_stru CV[], double **X, double **Y,
                    const double *cpu_time, const char *problem, const double time_plot[])
 {
@@ -552,27 +623,43 @@ void file_2D_write(const int n_x, const int n_y, const int N, const struct cell_
     example_io(problem, add_out, 0);
     const char *names[7] = {"RHO", "U", "V", "P", "E", "X", "Y"};
     for (int q = 0; q < 7; ++q) {
-        FILE *fp = open_output(add_out, names[q]);
-        for (int k = 0; k < N; ++k) {
-            for (int i = 0; i < n_y; ++i) {
-                for (int j = 0; j < n_x; ++j) {
-                    double v;
-                    switch (q) {
-                    case 0: v = CV[k].RHO[j][i]; break;
-                    case 1: v = CV[k].U[j][i]; break;
-                    case 2: v = CV[k].V[j][i]; break;
-                    case 3: v = CV[k].P[j][i]; break;
-                    case 4: v = CV[k].E[j][i]; break;
-                    case 5: v = 0.25 * (X[j][i] + X[j][i + 1] + X[j + 1][i] + X[j + 1][i + 1]); break;
-                    default: v = 0.25 * (Y[j][i] + Y[j][i + 1] + Y[j + 1][i] + Y[j + 1][i + 1]); break;
-                    }
-                    fprintf(fp, "%.10g\t", v);
-                }
-                fprintf(fp, "\n");
+        out_ctx o = {NULL, X, Y, q, 0};
+        hio_value_fn f = q < 5 ? val_2d : val_2d_center;
+        FILE *fp = out_text() ? open_output(add_out, names[q]) : NULL;
+        FILE *bp = NULL;
+        if (out_bin()) {
+            char file[PATH_LEN + 64];
+            snprintf(file, sizeof(file), "%s%s.bin", add_out, names[q]);
+            bp = hio_bin_create(file, 2, n_x, n_y, N, time_plot);
+            if (!bp) {
+                printf("Cannot open solution output file: %s!\n", names[q]);
+                exit(1);
             }
-            fprintf(fp, "\n\n");
         }
-        fclose(fp);
+        for (int k = 0; k < N; ++k) {
+            switch (q) {
+            case 0: o.a = CV[k].RHO; break;
+            case 1: o.a = CV[k].U; break;
+            case 2: o.a = CV[k].V; break;
+            case 3: o.a = CV[k].P; break;
+            case 4: o.a = CV[k].E; break;
+            default: break;
+            }
+            if (fp && (hio_write_text(fp, n_y, n_x, f, &o) || fprintf(fp, "\n\n") < 0)) {
+                printf("Error in writing solution output file: %s!\n", names[q]);
+                exit(1);
+            }
+            if (bp && hio_bin_plane(bp, n_y, n_x, f, &o)) {
+                printf("Error in writing solution output file: %s!\n", names[q]);
+                exit(1);
+            }
+        }
+        if (fp)
+            fclose(fp);
+        if (bp && fclose(bp) != 0) {
+            printf("Error in writing solution output file: %s!\n", names[q]);
+            exit(1);
+        }
     }
     write_time_plot(add_out, N, time_plot);
     config_write(add_out, cpu_time, problem);

@@ -11,6 +11,11 @@
  * ../../data_out/<dim>/<EUL_|LAG_|ALE_><order>_order/<name>/ (relative to the
  * driver's working directory, as in the reference; HYDRO_DATA_ROOT overrides
  * the "../../" prefix).
+ * Beyond the reference: the data files are read and the text written by
+ * several threads (hydro_fastio.h; the same numbers and bytes), an initial
+ * data file may also be <var>.bin (the binary FP64 format, used when no .txt
+ * or .dat exists), and config[302] = 1 adds binary output <var>.bin beside
+ * the .dat files, 2 writes only the binary files.
  */
 #ifndef HYDRO_IO_H
 #define HYDRO_IO_H
