@@ -2079,6 +2079,435 @@ done1:;
 /* point-solver entry points (golden vectors)                                 */
 /* ------------------------------------------------------------------------- */
 
+/* ------------------------------------------------------------------------- */
+/* 1D Lagrangian schemes                                                      */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * linear_GRP_solver_LAG, src/riemann_solver/linear_grp_solver_LAG.c:32-154
+ * (Ben-Artzi & Falcovitz's Lagrangian GRP): Ls/Rs = rho, u, p and the
+ * material derivatives t_rho, t_u, t_p.  D = (rho*_L, u, p, rho*_R)_t,
+ * U = (rho*_L, u*, p*, rho*_R).  The 3-rarefaction branch uses the left
+ * state's c_L, s_rho_L, s_p_L in its correction term (:128), as the
+ * reference does.
+ */
+static void orc_lag_solve(double gL, double gR, const double Ls[6], const double Rs[6], double eps, double atc,
+                          double D[4], double U[4])
+{
+    const double rho_L = Ls[0], u_L = Ls[1], p_L = Ls[2], s_rho_L = Ls[3], s_u_L = Ls[4], s_p_L = Ls[5];
+    const double rho_R = Rs[0], u_R = Rs[1], p_R = Rs[2], s_rho_R = Rs[3], s_u_R = Rs[4], s_p_R = Rs[5];
+    const double zetaL = (gL - 1.0) / (gL + 1.0);
+    const double zetaR = (gR - 1.0) / (gR + 1.0);
+    int CRW[2];
+    double c_L = sqrt(gL * p_L / rho_L), c_R = sqrt(gR * p_R / rho_R);
+    double g_L = rho_L * c_L, g_R = rho_R * c_R;
+    double u_star, p_star, rho_star_L, rho_star_R, c_star_L, c_star_R, g_star_L, g_star_R, beta_star;
+    double a_L, b_L, d_L, a_R, b_R, d_R, L_rho, L_u, L_p, A, B, W_L, W_R;
+
+    orc_exact(gL, gR, u_L, u_R, p_L, p_R, c_L, c_R, eps, eps, 500, &u_star, &p_star, CRW, NULL);
+    if (CRW[0]) {
+        rho_star_L = rho_L * pow(p_star / p_L, 1.0 / gL);
+        c_star_L = c_L * pow(p_star / p_L, 0.5 * (gL - 1.0) / gL);
+    } else {
+        rho_star_L = rho_L * (p_star + zetaL * p_L) / (p_L + zetaL * p_star);
+        c_star_L = sqrt(gL * p_star / rho_star_L);
+    }
+    if (CRW[1]) {
+        rho_star_R = rho_R * pow(p_star / p_R, 1.0 / gR);
+        c_star_R = c_R * pow(p_star / p_R, 0.5 * (gR - 1.0) / gR);
+    } else {
+        rho_star_R = rho_R * (p_star + zetaR * p_R) / (p_R + zetaR * p_star);
+        c_star_R = sqrt(gR * p_star / rho_star_R);
+    }
+    g_star_R = rho_star_R * c_star_R;
+    g_star_L = rho_star_L * c_star_L;
+
+    double dist = sqrt((u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
+    if (dist < atc) { /* acoustic case (:83-91) */
+        a_L = 1.0;
+        b_L = 1.0 / g_star_L;
+        d_L = -g_L * s_u_L - s_p_L;
+        a_R = -1.0;
+        b_R = 1.0 / g_star_R;
+        d_R = -g_R * s_u_R + s_p_R;
+    } else {
+        if (CRW[0]) { /* 1-rarefaction (:95-102) */
+            beta_star = g_star_L / g_L;
+            a_L = 1.0;
+            b_L = 1.0 / g_star_L;
+            d_L = (s_u_L + s_p_L / g_L) + 1.0 / g_L / (3.0 * gL - 1.0) * (c_L * c_L * s_rho_L - s_p_L) *
+                                              (pow(beta_star, (3.0 * gL - 1.0) / 2.0 / (gL + 1.0)) - 1.0);
+            d_L = -1.0 * sqrt(g_L * g_star_L) * d_L;
+        } else { /* 1-shock (:103-114) */
+            W_L = (p_star - p_L) / (u_star - u_L);
+            A = -0.5 / (p_star + zetaL * p_L);
+            a_L = 2.0 + A * (p_star - p_L);
+            b_L = -W_L / g_star_L / g_star_L - (a_L - 1.0) / W_L;
+            L_rho = (p_star - p_L) / 2.0 / rho_L;
+            B = 1.0 / (p_star - p_L) - zetaL * A;
+            L_u = rho_L * (u_star - u_L) * (gL * p_L * B + 0.5) + W_L;
+            L_p = 1.0 + B * (p_star - p_L);
+            d_L = L_u * s_u_L - L_p * s_p_L - L_rho * s_rho_L;
+        }
+        if (CRW[1]) { /* 3-rarefaction (:116-123) */
+            beta_star = g_star_R / g_R;
+            a_R = -1.0;
+            b_R = 1.0 / g_star_R;
+            d_R = (s_u_R - s_p_R / g_R) + 1.0 / g_R / (3.0 * gR - 1.0) * (-c_L * c_L * s_rho_L + s_p_L) *
+                                              (pow(beta_star, (3.0 * gR - 1.0) / 2.0 / (gR + 1.0)) - 1.0);
+            d_R = -1.0 * sqrt(g_R * g_star_R) * d_R;
+        } else { /* 3-shock (:124-135) */
+            W_R = (p_star - p_R) / (u_star - u_R);
+            A = -0.5 / (p_star + zetaR * p_R);
+            a_R = -2.0 - A * (p_star - p_R);
+            b_R = W_R / g_star_R / g_star_R - (a_R + 1.0) / W_R;
+            L_rho = (p_star - p_R) / 2.0 / rho_R;
+            B = 1.0 / (p_star - p_R) - zetaR * A;
+            L_u = rho_R * (u_R - u_star) * (gR * p_R * B + 0.5) - W_R;
+            L_p = 1.0 + B * (p_star - p_R);
+            d_R = L_u * s_u_R + L_p * s_p_R + L_rho * s_rho_R;
+        }
+    }
+    U[1] = u_star;
+    U[2] = p_star;
+    U[0] = rho_star_L;
+    U[3] = rho_star_R;
+    D[1] = (d_L * b_R - d_R * b_L) / (a_L * b_R - a_R * b_L);
+    D[2] = (d_L * a_R - d_R * a_L) / (b_L * a_R - b_R * a_L);
+    D[0] = D[2] / c_star_L / c_star_L;
+    D[3] = D[2] / c_star_R / c_star_R;
+}
+
+/* minmod_limiter on a moving grid (src/inter_process/slope_limiter.c:31-83,
+ * NO_h true): the differences are over half the distance of the neighbours'
+ * centres, the ghost cells having lengths HL, HR. */
+static void orc_minmod_moving(int m, int found, double alpha, double *s, const double *U, double UL, double UR,
+                              double HL, double HR, const double *X)
+{
+    for (int j = 0; j < m; ++j) {
+        double h, sL, sR;
+        if (j) {
+            h = 0.5 * (X[j + 1] - X[j - 1]);
+            sL = (U[j] - U[j - 1]) / h;
+        } else {
+            h = 0.5 * (X[j + 1] - X[j] + HL);
+            sL = (U[j] - UL) / h;
+        }
+        if (j < m - 1) {
+            h = 0.5 * (X[j + 2] - X[j]);
+            sR = (U[j + 1] - U[j]) / h;
+        } else {
+            h = 0.5 * (X[j + 1] - X[j] + HR);
+            sR = (UR - U[j]) / h;
+        }
+        s[j] = found ? orc_minmod3(alpha * sL, alpha * sR, s[j]) : orc_minmod2(sL, sR);
+    }
+}
+
+/*
+ * Godunov_solver_LAG_source (src/finite_volume/godunov_solver_LAG_source.c:28-243,
+ * order 1) and GRP_solver_LAG_source (src/finite_volume/grp_solver_LAG_source.c:28-355,
+ * order 2): cells carry fixed masses, the interfaces move with the star
+ * velocity, the time step is min(CFL h/c, 1.01 tau_prev).  Boundary values,
+ * ghost-cell lengths and slopes as bound_cond_slope_limiter with moving
+ * coordinates (src/inter_process/bound_cond_slope_limiter.c:30-136); the
+ * GRP checks run with config[8] = 1 as the 1D driver sets it for LAG
+ * (src/hydrocode_1D/hydrocode.c:238).  Two stored states (no plot times).
+ * X_out: the final m+1 node coordinates (may be NULL).
+ */
+int orc_run_1d_lag(int m, double *rho, double *u, double *p, double *E_out, double *X_out,
+                   const double *cfg_in, int ncfg, int order, double *info)
+{
+    double cfg[ORC_NCONF];
+    int j, k, q;
+    for (q = 0; q < ORC_NCONF; ++q)
+        cfg[q] = q < ncfg ? cfg_in[q] : INFINITY;
+    const double t_all = cfg[1], eps = cfg[4], gamma = cfg[6], CFL = cfg[7], h = cfg[10];
+    const int N = (int)cfg[5];
+    const int bound = (int)cfg[17];
+    const double alpha = cfg[41];
+    const double C_m = 1.01;
+    double tau = cfg[16];
+    double time_plot[2] = {0.0, t_all};
+
+    double *R[2], *Uv[2], *P[2], *Ev[2], *X[2];
+    for (k = 0; k < 2; ++k) {
+        R[k] = (double *)malloc(m * sizeof(double));
+        Uv[k] = (double *)malloc(m * sizeof(double));
+        P[k] = (double *)malloc(m * sizeof(double));
+        Ev[k] = (double *)malloc(m * sizeof(double));
+        X[k] = (double *)malloc((m + 1) * sizeof(double));
+    }
+    for (j = 0; j <= m; ++j)
+        X[0][j] = h * j;
+    for (j = 0; j < m; ++j) {
+        R[0][j] = rho[j];
+        Uv[0][j] = u[j];
+        P[0][j] = p[j];
+        Ev[0][j] = 0.5 * u[j] * u[j] + p[j] / (gamma - 1.0) / rho[j];
+    }
+    double *MASS = (double *)malloc(m * sizeof(double));
+    for (j = 0; j < m; ++j)
+        MASS[j] = h * R[0][j];
+    double *s_rho = (double *)calloc(m, sizeof(double)), *s_u = (double *)calloc(m, sizeof(double)),
+           *s_p = (double *)calloc(m, sizeof(double));
+    double *U_F = (double *)malloc((m + 1) * sizeof(double)), *P_F = (double *)malloc((m + 1) * sizeof(double));
+    double *U_next = (double *)malloc((m + 1) * sizeof(double)), *P_next = (double *)malloc((m + 1) * sizeof(double));
+    double *RL_next = (double *)malloc((m + 1) * sizeof(double)), *RR_next = (double *)malloc((m + 1) * sizeof(double));
+    double *U_t = (double *)malloc((m + 1) * sizeof(double)), *P_t = (double *)malloc((m + 1) * sizeof(double));
+    double *RL_t = (double *)malloc((m + 1) * sizeof(double)), *RR_t = (double *)malloc((m + 1) * sizeof(double));
+    /* ghost cells: rho, u, p, srho, su, sp, H (the reference's b_f_var starts with zero slopes, H = h) */
+    double gL[7] = {0, 0, 0, 0, 0, 0, h}, gR[7] = {0, 0, 0, 0, 0, 0, h};
+    int nt = 0, stop_t = 0, found = 0;
+    double time_c = 0.0, cpu_sum = 0.0, cpu_time[2] = {0.0, 0.0};
+    double t_start = wall_clock();
+
+    for (k = 1; k <= N; ++k) {
+        double tic = wall_clock();
+        if (time_c >= time_plot[nt] && nt < 1) {
+            for (j = 0; j < m; ++j) {
+                R[nt + 1][j] = R[nt][j];
+                Uv[nt + 1][j] = Uv[nt][j];
+                Ev[nt + 1][j] = Ev[nt][j];
+                P[nt + 1][j] = P[nt][j];
+                X[nt + 1][j] = X[nt][j];
+            }
+            X[nt + 1][m] = X[nt][m];
+            nt++;
+        }
+        double *r = R[nt], *uu = Uv[nt], *pp = P[nt], *ee = Ev[nt], *x = X[nt];
+        double h_S_max = INFINITY;
+
+        /* boundary values and ghost lengths (bound_cond_slope_limiter.c:41-106) */
+        switch (bound) {
+        case -1:
+            if (!found) {
+                gL[1] = Uv[0][0]; gR[1] = Uv[0][m - 1];
+                gL[2] = P[0][0]; gR[2] = P[0][m - 1];
+                gL[0] = R[0][0]; gR[0] = R[0][m - 1];
+            }
+            gL[6] = h; gR[6] = h;
+            break;
+        case -2:
+            gL[1] = -uu[0]; gR[1] = -uu[m - 1];
+            gL[2] = pp[0]; gR[2] = pp[m - 1];
+            gL[0] = r[0]; gR[0] = r[m - 1];
+            gL[6] = x[1] - x[0]; gR[6] = x[m] - x[m - 1];
+            break;
+        case -4:
+            gL[1] = uu[0]; gR[1] = uu[m - 1];
+            gL[2] = pp[0]; gR[2] = pp[m - 1];
+            gL[0] = r[0]; gR[0] = r[m - 1];
+            gL[6] = x[1] - x[0]; gR[6] = x[m] - x[m - 1];
+            break;
+        case -7:
+            gL[1] = uu[m - 1]; gR[1] = uu[0];
+            gL[2] = pp[m - 1]; gR[2] = pp[0];
+            gL[0] = r[m - 1]; gR[0] = r[0];
+            gL[6] = x[m] - x[m - 1]; gR[6] = x[1] - x[0];
+            break;
+        case -24:
+            gL[1] = -uu[0]; gR[1] = uu[m - 1];
+            gL[2] = pp[0]; gR[2] = pp[m - 1];
+            gL[0] = r[0]; gR[0] = r[m - 1];
+            gL[6] = x[1] - x[0]; gR[6] = x[m] - x[m - 1];
+            break;
+        default:
+            goto done_lag;
+        }
+        if (order == 2) {
+            orc_minmod_moving(m, found, alpha, s_u, uu, gL[1], gR[1], gL[6], gR[6], x);
+            orc_minmod_moving(m, found, alpha, s_p, pp, gL[2], gR[2], gL[6], gR[6], x);
+            orc_minmod_moving(m, found, alpha, s_rho, r, gL[0], gR[0], gL[6], gR[6], x);
+            switch (bound) {
+            case -2:
+                gL[4] = s_u[0]; gR[4] = s_u[m - 1];
+                break;
+            case -7:
+                gL[4] = s_u[m - 1]; gR[4] = s_u[0];
+                gL[5] = s_p[m - 1]; gR[5] = s_p[0];
+                gL[3] = s_rho[m - 1]; gR[3] = s_rho[0];
+                break;
+            case -24:
+                gL[4] = s_u[0];
+                break;
+            }
+        }
+        found = 1;
+
+        for (j = 0; j <= m; ++j) {
+            double Ls[6], Rs[6], h_L, h_R;
+            const double *cL_ = j ? NULL : gL, *cR_ = j < m ? NULL : gR;  /* ghost or cell */
+            h_L = j ? x[j] - x[j - 1] : gL[6];
+            h_R = j < m ? x[j + 1] - x[j] : gR[6];
+            if (order == 1) { /* cell values (godunov_solver_LAG_source.c:103-128) */
+                Ls[0] = cL_ ? cL_[0] : r[j - 1];
+                Ls[1] = cL_ ? cL_[1] : uu[j - 1];
+                Ls[2] = cL_ ? cL_[2] : pp[j - 1];
+                Rs[0] = cR_ ? cR_[0] : r[j];
+                Rs[1] = cR_ ? cR_[1] : uu[j];
+                Rs[2] = cR_ ? cR_[2] : pp[j];
+            } else { /* grp_solver_LAG_source.c:137-162; the right ghost with '+' as there */
+                if (j) {
+                    Ls[0] = r[j - 1] + 0.5 * h_L * s_rho[j - 1];
+                    Ls[1] = uu[j - 1] + 0.5 * h_L * s_u[j - 1];
+                    Ls[2] = pp[j - 1] + 0.5 * h_L * s_p[j - 1];
+                } else {
+                    Ls[0] = gL[0] + 0.5 * h_L * gL[3];
+                    Ls[1] = gL[1] + 0.5 * h_L * gL[4];
+                    Ls[2] = gL[2] + 0.5 * h_L * gL[5];
+                }
+                if (j < m) {
+                    Rs[0] = r[j] - 0.5 * h_R * s_rho[j];
+                    Rs[1] = uu[j] - 0.5 * h_R * s_u[j];
+                    Rs[2] = pp[j] - 0.5 * h_R * s_p[j];
+                } else {
+                    Rs[0] = gR[0] + 0.5 * h_R * gR[3];
+                    Rs[1] = gR[1] + 0.5 * h_R * gR[4];
+                    Rs[2] = gR[2] + 0.5 * h_R * gR[5];
+                }
+            }
+            double c_L = sqrt(gamma * Ls[2] / Ls[0]);
+            double c_R = sqrt(gamma * Rs[2] / Rs[0]);
+            h_S_max = fmin(h_S_max, h_L / c_L);
+            h_S_max = fmin(h_S_max, h_R / c_R);
+            if ((bound == -2 || bound == -24) && j == 0)
+                h_S_max = fmin(h_S_max, h_L / (fabs(Ls[1]) + c_L));
+            if (bound == -2 && j == m)
+                h_S_max = fmin(h_S_max, h_R / (fabs(Rs[1]) + c_R));
+
+            if (order == 1) { /* godunov_solver_LAG_source.c:137-152 */
+                double us, ps;
+                int crw[2];
+                orc_exact(gamma, gamma, Ls[1], Rs[1], Ls[2], Rs[2], c_L, c_R, eps, eps, 500, &us, &ps, crw, NULL);
+                if (ps < eps)
+                    stop_t = 1;
+                if (!isfinite(ps) || !isfinite(us))
+                    stop_t = 1;
+                U_F[j] = us;
+                P_F[j] = ps;
+                continue;
+            }
+            /* material derivatives (grp_solver_LAG_source.c:173-198) */
+            double dL[3], dR[3]; /* rho, u, p */
+            if (j) { dL[1] = s_u[j - 1]; dL[2] = s_p[j - 1]; dL[0] = s_rho[j - 1]; }
+            else { dL[0] = gL[3]; dL[1] = gL[4]; dL[2] = gL[5]; }
+            if (j < m) { dR[1] = s_u[j]; dR[2] = s_p[j]; dR[0] = s_rho[j]; }
+            else { dR[0] = gR[3]; dR[1] = gR[4]; dR[2] = gR[5]; }
+            /* ifvar_check dim 1 aborts the run (:199-203) */
+            if (Ls[2] < eps || Rs[2] < eps || Ls[0] < eps || Rs[0] < eps || !isfinite(dL[2]) || !isfinite(dR[2]) ||
+                !isfinite(dL[1]) || !isfinite(dR[1]) || !isfinite(dL[0]) || !isfinite(dR[0]))
+                goto done_lag;
+            Ls[4] = dL[1] / Ls[0];
+            Ls[5] = dL[2] / Ls[0];
+            Ls[3] = dL[0] / Ls[0];
+            Rs[4] = dR[1] / Rs[0];
+            Rs[5] = dR[2] / Rs[0];
+            Rs[3] = dR[0] / Rs[0];
+            double D[4], Ust[4];
+            orc_lag_solve(gamma, gamma, Ls, Rs, eps, eps, D, Ust);
+            /* star_dire_check dim 1 with config[8] = 1 (fluid_var_check.c:72-90) */
+            if (Ust[2] < eps || Ust[0] < eps || Ust[3] < eps || !isfinite(Ust[1]) || !isfinite(Ust[2]) ||
+                !isfinite(Ust[0]) || !isfinite(Ust[3]) || !isfinite(D[1]) || !isfinite(D[2]) || !isfinite(D[0]) ||
+                !isfinite(D[3]))
+                stop_t = 1;
+            RL_next[j] = Ust[0];
+            RR_next[j] = Ust[3];
+            U_next[j] = Ust[1];
+            P_next[j] = Ust[2];
+            RL_t[j] = D[0];
+            RR_t[j] = D[3];
+            U_t[j] = D[1];
+            P_t[j] = D[2];
+        }
+
+        if (isfinite(t_all) || !isfinite(cfg[16]) || cfg[16] <= 0.0) {
+            tau = fmin(CFL * h_S_max, C_m * tau);
+            if (tau < eps)
+                stop_t = 1;
+            else if ((time_c + tau) > (t_all - eps))
+                tau = t_all - time_c;
+            else if (!isfinite(tau))
+                goto done_lag;
+        }
+        for (j = 0; j <= m; ++j) {
+            if (order == 2) {
+                U_F[j] = U_next[j] + 0.5 * tau * U_t[j];
+                P_F[j] = P_next[j] + 0.5 * tau * P_t[j];
+                RL_next[j] += tau * RL_t[j];
+                RR_next[j] += tau * RR_t[j];
+                U_next[j] += tau * U_t[j];
+                P_next[j] += tau * P_t[j];
+            }
+            x[j] += tau * U_F[j];
+        }
+        for (j = 0; j < m; ++j) {
+            r[j] = 1.0 / (1.0 / r[j] + tau / MASS[j] * (U_F[j + 1] - U_F[j]));
+            uu[j] = uu[j] - tau / MASS[j] * (P_F[j + 1] - P_F[j]);
+            ee[j] = ee[j] - tau / MASS[j] * (P_F[j + 1] * U_F[j + 1] - P_F[j] * U_F[j]);
+            pp[j] = (ee[j] - 0.5 * uu[j] * uu[j]) * (gamma - 1.0) * r[j];
+            if (pp[j] < eps || r[j] < eps)
+                stop_t = 1;
+            if (order == 2) {
+                s_u[j] = (U_next[j + 1] - U_next[j]) / (x[j + 1] - x[j]);
+                s_p[j] = (P_next[j + 1] - P_next[j]) / (x[j + 1] - x[j]);
+                s_rho[j] = (RL_next[j + 1] - RR_next[j]) / (x[j + 1] - x[j]);
+            }
+        }
+        time_c += tau;
+        if (stop_t || time_c > (t_all - eps) || !isfinite(time_c))
+            break;
+        double toc = wall_clock();
+        cpu_sum += toc - tic;
+        cpu_time[nt] = cpu_sum;
+    }
+done_lag:;
+    double t_end = wall_clock();
+    if (isfinite(time_c))
+        time_plot[nt] = time_c;
+    else if (isfinite(t_all))
+        time_plot[nt] = t_all;
+    else if (isfinite(tau))
+        time_plot[nt] = k * tau;
+    for (j = 0; j < m; ++j) {
+        rho[j] = R[nt][j];
+        u[j] = Uv[nt][j];
+        p[j] = P[nt][j];
+        if (E_out)
+            E_out[j] = Ev[nt][j];
+    }
+    if (X_out)
+        for (j = 0; j <= m; ++j)
+            X_out[j] = X[nt][j];
+    if (info) {
+        info[0] = (double)k;
+        info[1] = time_plot[nt];
+        info[2] = cpu_time[nt];
+        info[3] = t_end - t_start;
+    }
+    for (k = 0; k < 2; ++k) {
+        free(R[k]); free(Uv[k]); free(P[k]); free(Ev[k]); free(X[k]);
+    }
+    free(MASS); free(s_rho); free(s_u); free(s_p); free(U_F); free(P_F);
+    free(U_next); free(P_next); free(RL_next); free(RR_next); free(U_t); free(P_t); free(RL_t); free(RR_t);
+    return 0;
+}
+
+/* linear_GRP_solver_LAG on cnt interfaces; layout as ref_lag in ref_harness.c. */
+void orc_lag(int cnt, const double *in, double eps, double atc, double *out)
+{
+    for (int q = 0; q < cnt; ++q) {
+        const double *a = in + 13 * q;
+        double D[4], U[4];
+        orc_lag_solve(a[0], a[0], a + 1, a + 7, eps, atc, D, U);
+        double *o = out + 8 * q;
+        for (int k2 = 0; k2 < 4; ++k2) {
+            o[k2] = D[k2];
+            o[4 + k2] = U[k2];
+        }
+    }
+}
+
 void orc_riemann_exact(int cnt, const double *in, double eps, double tol, int N, double *out)
 {
     for (int q = 0; q < cnt; ++q) {

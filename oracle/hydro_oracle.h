@@ -27,6 +27,9 @@ void orc_riemann_exact_ben(int cnt, const double *in, double eps, double tol, in
 void orc_grp2d_flux(int cnt, const double *in, double tau, double eps, double *out);
 void orc_q1d(int cnt, const double *in, double eps, double atc, double *out);
 void orc_g2d(int cnt, const double *in, double eps, double atc, double *out);
+int orc_run_1d_lag(int m, double *rho, double *u, double *p, double *E_out, double *X_out,
+                   const double *cfg_in, int ncfg, int order, double *info);
+void orc_lag(int cnt, const double *in, double eps, double atc, double *out);
 void orc_grp1d(int cnt, const double *in, double eps, double atc, double *out);
 
 /* Newton iteration count of the exact solver (same inputs as orc_riemann_exact);

@@ -99,6 +99,10 @@ class Oracle:
         self._flux.argtypes = [_int, _dp, _dbl, _dbl, _dp]
         self._q1d = getattr(L, p + "q1d")
         self._q1d.argtypes = [_int, _dp, _dbl, _dbl, _dp]
+        self._run1dl = getattr(L, p + "run_1d_lag")
+        self._run1dl.argtypes = [_int, _dp, _dp, _dp, _dp, _dp, _dp, _int, _int, _dp]
+        self._lag = getattr(L, p + "lag")
+        self._lag.argtypes = [_int, _dp, _dbl, _dbl, _dp]
         self._g2d = getattr(L, p + "g2d")
         self._g2d.argtypes = [_int, _dp, _dbl, _dbl, _dp]
         self._g1d = getattr(L, p + "grp1d")
@@ -170,6 +174,25 @@ class Oracle:
         inp = np.ascontiguousarray(inp, np.float64)
         out = np.zeros((len(inp), 14))
         self._q1d(len(inp), inp, eps, atc, out)
+        return out
+
+    def run_1d_lag(self, rho, u, p, cfg, order):
+        """1D Lagrangian run (order 1 Godunov, 2 GRP); returns the final state,
+        the m+1 node coordinates and the step/time summary."""
+        m = len(rho)
+        r, uu, pp = (np.ascontiguousarray(a, np.float64).copy() for a in (rho, u, p))
+        E = np.zeros(m)
+        X = np.zeros(m + 1)
+        info = np.zeros(4)
+        cfg = np.ascontiguousarray(cfg, np.float64)
+        self._run1dl(m, r, uu, pp, E, X, cfg, len(cfg), int(order), info)
+        return {"rho": r, "u": uu, "p": pp, "E": E, "X": X, "steps": info[0], "time": info[1], "wall": info[3]}
+
+    def lag(self, inp, eps=1e-9, atc=1e-9):
+        """linear_GRP_solver_LAG on rows (gamma, left rho,u,p,t_rho,t_u,t_p, right the same)."""
+        inp = np.ascontiguousarray(inp, np.float64)
+        out = np.zeros((len(inp), 8))
+        self._lag(len(inp), inp, eps, atc, out)
         return out
 
     def g2d(self, inp, eps=1e-9, atc=1e-9):

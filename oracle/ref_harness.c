@@ -354,6 +354,93 @@ void ref_q1d(int cnt, const double *in, double eps, double atc, double *out)
     }
 }
 
+/*
+ * 1D Lagrangian run (order 1 = Godunov_solver_LAG_source, 2 = GRP_solver_LAG_source),
+ * set up as src/hydrocode_1D/hydrocode.c:196-247 does for "LAG": node
+ * coordinates X[0][j] = j h, config[8] = 1.  rho/u/p in, final state out;
+ * E_out and X_out (m+1 node coordinates) may be NULL.  info as in ref_run_1d.
+ */
+int ref_run_1d_lag(int m, double *rho, double *u, double *p, double *E_out, double *X_out,
+                   const double *cfg, int ncfg, int order, double *info)
+{
+    int j;
+    load_config(cfg, ncfg);
+    config[0] = 1.0;
+    config[8] = 1.0;
+    const double gamma = config[6], h = config[10];
+    int N_plot = 2;
+    double time_plot[2] = {0.0, config[1]};
+    int N = 2;
+    struct cell_var_stru CV;
+    memset(&CV, 0, sizeof(CV));
+    CV.RHO = alloc2(N, m);
+    CV.U = alloc2(N, m);
+    CV.P = alloc2(N, m);
+    CV.E = alloc2(N, m);
+    double **X = alloc2(N, m + 1);
+    for (j = 0; j <= m; ++j)
+        X[0][j] = h * j;
+    for (j = 0; j < m; ++j) {
+        CV.RHO[0][j] = rho[j];
+        CV.U[0][j] = u[j];
+        CV.P[0][j] = p[j];
+        CV.E[0][j] = 0.5 * CV.U[0][j] * CV.U[0][j] + CV.P[0][j] / (gamma - 1.0) / CV.RHO[0][j];
+    }
+    double cpu_time[2] = {0.0, 0.0};
+    double t0 = wall();
+    if (order == 1)
+        Godunov_solver_LAG_source(m, CV, X, cpu_time, &N_plot, time_plot);
+    else
+        GRP_solver_LAG_source(m, CV, X, cpu_time, &N_plot, time_plot);
+    double t1 = wall();
+    int last = N_plot - 1;
+    for (j = 0; j < m; ++j) {
+        rho[j] = CV.RHO[last][j];
+        u[j] = CV.U[last][j];
+        p[j] = CV.P[last][j];
+        if (E_out)
+            E_out[j] = CV.E[last][j];
+    }
+    if (X_out)
+        for (j = 0; j <= m; ++j)
+            X_out[j] = X[last][j];
+    if (info) {
+        info[0] = config[5];
+        info[1] = time_plot[last];
+        info[2] = cpu_time[last];
+        info[3] = t1 - t0;
+    }
+    free2(CV.RHO, N);
+    free2(CV.U, N);
+    free2(CV.P, N);
+    free2(CV.E, N);
+    free2(X, N);
+    return 0;
+}
+
+/* linear_GRP_solver_LAG (linear_grp_solver_LAG.c:32) on cnt interfaces.
+ * in: cnt x 13 = gamma, left rho,u,p,t_rho,t_u,t_p (material derivatives),
+ * right the same.  out: cnt x 8 = D[0..3], U[0..3]. */
+void ref_lag(int cnt, const double *in, double eps, double atc, double *out)
+{
+    for (int q = 0; q < cnt; ++q) {
+        const double *a = in + 13 * q;
+        struct i_f_var L, R;
+        memset(&L, 0, sizeof(L));
+        memset(&R, 0, sizeof(R));
+        L.gamma = R.gamma = a[0];
+        L.RHO = a[1]; L.U = a[2]; L.P = a[3]; L.t_rho = a[4]; L.t_u = a[5]; L.t_p = a[6];
+        R.RHO = a[7]; R.U = a[8]; R.P = a[9]; R.t_rho = a[10]; R.t_u = a[11]; R.t_p = a[12];
+        double D[4], U[4];
+        linear_GRP_solver_LAG(D, U, &L, &R, eps, atc);
+        double *o = out + 8 * q;
+        for (int k = 0; k < 4; ++k) {
+            o[k] = D[k];
+            o[4 + k] = U[k];
+        }
+    }
+}
+
 /* linear_GRP_solver_Edir_G2D (linear_grp_solver_Edir_G2D.c:48); layout as ref_q1d. */
 void ref_g2d(int cnt, const double *in, double eps, double atc, double *out)
 {

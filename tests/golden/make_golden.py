@@ -8,6 +8,7 @@ reference tree; the fixtures travel with the repository.
     python tests/golden/make_golden.py            # all fixtures
     python tests/golden/make_golden.py --large    # also the 1024^2 x 500 run summary
     python tests/golden/make_golden.py --only g2d # only the genuinely-2D solver's fixtures
+    python tests/golden/make_golden.py --only lag # only the 1D Lagrangian schemes' fixtures
 
 The genuinely-2D GRP fixtures come from oracle/_ref/libhydro_ref_g2d.so, the
 same sources with GRP_2D_flux calling linear_GRP_solver_Edir_G2D (the
@@ -139,14 +140,71 @@ def make_g2d():
     np.savez_compressed(os.path.join(HERE, "runs_2d_g2d.npz"), **runs)
 
 
+def lag_inputs(rng, n):
+    """Lagrangian GRP pairs: rho, u, p and material derivatives per side;
+    shocks, rarefactions and near-uniform (acoustic) pairs."""
+    def side(k):
+        return np.column_stack([np.exp(rng.uniform(-2, 2, k)), rng.uniform(-2, 2, k), np.exp(rng.uniform(-2, 2, k)),
+                                rng.normal(0, 1, (k, 3))])
+    L, R = side(n), side(n)
+    k = n // 6
+    R[:k, :3] = L[:k, :3]                                            # equal states: acoustic
+    L[k:2 * k, 1] = 2.0; R[k:2 * k, 1] = -2.0                        # colliding: two shocks
+    L[2 * k:3 * k, 1] = -1.5; R[2 * k:3 * k, 1] = 1.5                # receding: two rarefactions
+    return np.column_stack([np.full(n, G), L, R])
+
+
+def lag_runs():
+    """Sod (400 cells, t = 0.2) with both Lagrangian schemes, and a smooth
+    profile with a jump under every boundary code."""
+    runs = []
+    for order in (1, 2):
+        rho, u, p = cases.sod(400)
+        cfg = orc.default_config_1d(t_all=0.2, steps=100000, hx=1 / 400, bx=-4, cfl=0.45)
+        runs.append((f"sod{order}", rho, u, p, cfg, order))
+    m = 120
+    x = (np.arange(m) + 0.5) / m
+    rho = 1.0 + 0.5 * np.sin(2 * np.pi * x) + (x > 0.3) * 0.4
+    u = 0.3 * np.cos(2 * np.pi * x)
+    p = 1.0 + 0.2 * (x < 0.6)
+    for bnd, order in ((-7, 2), (-2, 2), (-24, 1), (-1, 2), (-2, 1), (-24, 2)):
+        cfg = orc.default_config_1d(t_all=0.1, steps=100000, hx=1 / m, bx=bnd, cfl=0.45)
+        runs.append((f"bc{-bnd}o{order}", rho, u, p, cfg, order))
+    # a fixed time step (config[16]) with a step count and no end time
+    cfg = orc.default_config_1d(t_all=-1, steps=60, hx=1 / m, bx=-4, cfl=0.45)
+    cfg[16] = 4e-4
+    runs.append(("fixed_tau", rho, u, p, cfg, 2))
+    return runs
+
+
+def make_lag():
+    R = orc.Oracle("reference")
+    rng = np.random.default_rng(20261204)
+    lin = lag_inputs(rng, 1200)
+    np.savez_compressed(os.path.join(HERE, "lag.npz"), inp=lin, out=R.lag(lin, 1e-9, 1e-9),
+                        out_acoustic=R.lag(lin, 1e-9, np.inf))
+    r1 = {}
+    for name, rho, u, p, cfg, order in lag_runs():
+        out = R.run_1d_lag(rho, u, p, cfg, order)
+        r1[f"{name}/in"] = np.stack([rho, u, p])
+        r1[f"{name}/cfg"] = cfg
+        for f in ("rho", "u", "p", "E", "X"):
+            r1[f"{name}/{f}"] = out[f]
+        r1[f"{name}/meta"] = np.array([out["steps"], out["time"], order])
+    np.savez_compressed(os.path.join(HERE, "runs_1d_lag.npz"), **r1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
-    ap.add_argument("--only", choices=["all", "g2d"], default="all")
+    ap.add_argument("--only", choices=["all", "g2d", "lag"], default="all")
     args = ap.parse_args()
     orc.build(ref=True)
-    make_g2d()
-    if args.only == "g2d":
+    if args.only in ("all", "g2d"):
+        make_g2d()
+    if args.only in ("all", "lag"):
+        make_lag()
+    if args.only != "all":
         print("fixtures written to", HERE)
         return
     R = orc.Oracle("reference")

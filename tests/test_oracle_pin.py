@@ -182,3 +182,56 @@ def test_g2d_port_matches_reference_random(port, ref_g2d):
     a, b = port.run_2d(rho, u, v, p, cfg), ref_g2d.run_2d(rho, u, v, p, cfg)
     for f in ("rho", "u", "v", "p", "E"):
         assert np.array_equal(a[f], b[f])
+
+
+def test_lag_golden(port):
+    """linear_GRP_solver_LAG, nonlinear and acoustic modes, bit for bit."""
+    d = load("lag.npz")
+    assert np.array_equal(port.lag(d["inp"], 1e-9, 1e-9), d["out"], equal_nan=True)
+    assert np.array_equal(port.lag(d["inp"], 1e-9, np.inf), d["out_acoustic"], equal_nan=True)
+
+
+def test_runs_1d_lag_golden(port):
+    """Godunov_solver_LAG_source / GRP_solver_LAG_source: Sod and every
+    boundary code, state and moving node coordinates bit for bit."""
+    d = load("runs_1d_lag.npz")
+    names = _runs(d)
+    assert len(names) >= 9
+    for name in names:
+        rho, u, p = d[f"{name}/in"]
+        meta = d[f"{name}/meta"]
+        out = port.run_1d_lag(rho, u, p, d[f"{name}/cfg"], int(meta[2]))
+        assert out["steps"] == meta[0] and out["time"] == meta[1], name
+        for f in ("rho", "u", "p", "E", "X"):
+            assert np.array_equal(out[f], d[f"{name}/{f}"]), (name, f)
+
+
+def test_lag_sod_known_answer(port):
+    """Sod in Lagrangian coordinates: the contact moves at u* = 0.92745, so the
+    node that starts at x = 0.5 ends at 0.5 + 0.2 u*; the plateau pressure is
+    p* = 0.30313 (Toro, table 4.3)."""
+    d = load("runs_1d_lag.npz")
+    for order in (1, 2):
+        X = d[f"sod{order}/X"]
+        assert abs(X[200] - (0.5 + 0.2 * 0.92745)) < 2e-3
+        p = d[f"sod{order}/p"]
+        assert abs(p[200] - 0.30313) < 5e-3
+
+
+def test_lag_port_matches_reference_random(port, ref):
+    rng = np.random.default_rng(77)
+    n = 800
+    side = lambda: np.column_stack([np.exp(rng.uniform(-3, 3, n)), rng.uniform(-3, 3, n), np.exp(rng.uniform(-3, 3, n)),
+                                    rng.normal(0, 2, (n, 3))])
+    inp = np.column_stack([np.full(n, 1.4), side(), side()])
+    assert np.array_equal(port.lag(inp), ref.lag(inp), equal_nan=True)
+    import oracle as orc
+
+    m = 90
+    x = (np.arange(m) + 0.5) / m
+    rho, u, p = 1 + 0.3 * np.cos(4 * np.pi * x), 0.2 * np.sin(2 * np.pi * x), 1 + 0.5 * (x > 0.45)
+    for order in (1, 2):
+        cfg = orc.default_config_1d(t_all=0.08, steps=100000, hx=1 / m, bx=-7, cfl=0.4)
+        a, b = port.run_1d_lag(rho, u, p, cfg, order), ref.run_1d_lag(rho, u, p, cfg, order)
+        for f in ("rho", "u", "p", "E", "X"):
+            assert np.array_equal(a[f], b[f])
