@@ -1,13 +1,13 @@
 /*
- * hydrocode_1D.c -- 1D Eulerian driver linked against libhydro_gb300.so.
+ * hydrocode_1D.c -- 1D driver linked against libhydro_gb300.so.
  *
- *   hydrocode_1D.out <in_example> <out_name> <order[_scheme]> EUL [n=C ...]
+ *   hydrocode_1D.out <in_example> <out_name> <order[_scheme]> EUL|LAG [n=C ...]
  *
  * Same command line, input folder, configuration and set-up as the
- * reference's src/hydrocode_1D/hydrocode.c:150-439 for the Eulerian schemes
- * (order 1: Godunov with the exact Riemann solver, order 2: GRP); the
- * Lagrangian schemes are not part of this library.  Exit codes as in the
- * reference.  NODATPLOT suppresses the .dat output.
+ * reference's src/hydrocode_1D/hydrocode.c:150-439: order 1 Godunov with the
+ * exact Riemann solver, order 2 GRP, on Eulerian (EUL) or Lagrangian (LAG,
+ * moving nodes X[k]) coordinates.  Exit codes as in the reference.
+ * NODATPLOT suppresses the .dat output.
  */
 #include <math.h>
 #include <stdio.h>
@@ -63,23 +63,37 @@ int main(int argc, char *argv[])
         X[0][j] = h * j;
     for (int j = 0; j < m; ++j)
         CV.E[0][j] = 0.5 * CV.U[0][j] * CV.U[0][j] + CV.P[0][j] / (gamma - 1.0) / CV.RHO[0][j];
-    if (strcmp(argv[4], "EUL") != 0) {
+    if (strcmp(argv[4], "LAG") == 0) { /* hydrocode.c:237-251 */
+        config[8] = 1.0;
+        switch (order) {
+        case 1:
+            Godunov_solver_LAG_source(m, CV, X, cpu_time, &N, time_plot);
+            break;
+        case 2:
+            GRP_solver_LAG_source(m, CV, X, cpu_time, &N, time_plot);
+            break;
+        default:
+            printf("NOT appropriate order of the scheme! The order is %d.\n", order);
+            return 4;
+        }
+    } else if (strcmp(argv[4], "EUL") == 0) { /* hydrocode.c:252-270 */
+        config[8] = 0.0;
+        for (int k = 1; k < N; ++k)
+            for (int j = 0; j <= m; ++j)
+                X[k][j] = X[0][j];
+        switch (order) {
+        case 1:
+            Godunov_solver_EUL_source(m, CV, cpu_time, &N, time_plot);
+            break;
+        case 2:
+            GRP_solver_EUL_source(m, CV, cpu_time, &N, time_plot);
+            break;
+        default:
+            printf("NOT appropriate order of the scheme! The order is %d.\n", order);
+            return 4;
+        }
+    } else {
         printf("NOT appropriate coordinate framework! The framework is %s.\n", argv[4]);
-        return 4;
-    }
-    config[8] = 0.0;
-    for (int k = 1; k < N; ++k)
-        for (int j = 0; j <= m; ++j)
-            X[k][j] = X[0][j];
-    switch (order) {
-    case 1:
-        Godunov_solver_EUL_source(m, CV, cpu_time, &N, time_plot);
-        break;
-    case 2:
-        GRP_solver_EUL_source(m, CV, cpu_time, &N, time_plot);
-        break;
-    default:
-        printf("NOT appropriate order of the scheme! The order is %d.\n", order);
         return 4;
     }
 #ifndef NODATPLOT

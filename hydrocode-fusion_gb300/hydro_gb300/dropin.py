@@ -111,3 +111,42 @@ def call_1d(lib, rho, u, p, gamma, cfg, order, plot_times=None, N_MAX=1000):
     fn.argtypes = [ctypes.c_int, CellVarStru, P, ctypes.POINTER(ctypes.c_int), P]
     fn(m, cv, cpu_time.ctypes.data_as(P), ctypes.byref(nplot), time_plot.ctypes.data_as(P))
     return data, nplot.value, time_plot, conf[5]
+
+
+def call_1d_lag(lib, rho, u, p, gamma, cfg, order, plot_times=None, N_MAX=1000):
+    """Run Godunov_solver_LAG_source / GRP_solver_LAG_source with the 1D driver's
+    set-up for "LAG" (src/hydrocode_1D/hydrocode.c:196-247: X[0][j] = j h,
+    config[8] = 1).  Returns (CV data [4][N][m], node slots X [N][m+1], N_plot,
+    time_plot, config[5])."""
+    m = len(rho)
+    ntp = 0 if plot_times is None else len(plot_times)
+    N_plot = ntp + 2
+    N = min(N_MAX, N_plot)
+    time_plot = np.zeros(N_plot)
+    time_plot[-1] = cfg[1]
+    if ntp:
+        time_plot[1:-1] = plot_times
+    data = np.zeros((4, N, m))
+    data[0, 0], data[1, 0], data[2, 0] = rho, u, p
+    data[3, 0] = 0.5 * u * u + p / (gamma - 1.0) / rho
+    X = np.zeros((N, m + 1))
+    X[0] = cfg[10] * np.arange(m + 1)
+    keep = []
+    cv = CellVarStru()
+    cv.RHO = _rows(data[0], keep)
+    cv.U = _rows(data[1], keep)
+    cv.P = _rows(data[2], keep)
+    cv.E = _rows(data[3], keep)
+    xrows = _rows(X, keep)
+    conf = config_view(lib)
+    conf[:] = cfg
+    conf[8] = 1.0
+    cpu_time = np.zeros(N)
+    nplot = ctypes.c_int(N)
+    fn = lib.Godunov_solver_LAG_source if order == 1 else lib.GRP_solver_LAG_source
+    fn.restype = None
+    fn.argtypes = [ctypes.c_int, CellVarStru, ctypes.c_void_p, P, ctypes.POINTER(ctypes.c_int), P]
+    fn(m, cv, ctypes.cast(xrows, ctypes.c_void_p), cpu_time.ctypes.data_as(P), ctypes.byref(nplot),
+       time_plot.ctypes.data_as(P))
+    return data, X, nplot.value, time_plot, conf[5]
+

@@ -64,6 +64,17 @@ void Godunov_solver_EUL_source(const int m, struct cell_var_stru CV, double *cpu
 void GRP_solver_EUL_source(const int m, struct cell_var_stru CV, double *cpu_time, int *N_plot,
                            double time_plot[]);
 
+/* 1D first-order Lagrangian Godunov scheme: cells keep their masses, the
+ * nodes X[k][0..m] move with the star velocity (X[0] holds the initial nodes).
+ * Replaces src/finite_volume/godunov_solver_LAG_source.c:28 (finite_volume.h:16). */
+void Godunov_solver_LAG_source(const int m, struct cell_var_stru CV, double *X[], double *cpu_time, int *N_plot,
+                               double time_plot[]);
+
+/* 1D second-order Lagrangian GRP scheme.
+ * Replaces src/finite_volume/grp_solver_LAG_source.c:28 (finite_volume.h:20). */
+void GRP_solver_LAG_source(const int m, struct cell_var_stru CV, double *X[], double *cpu_time, int *N_plot,
+                           double time_plot[]);
+
 /* 2D unsplit GRP scheme.  CV[k].RHO/U/V/P/E[j][i] (x-major), k < N_T.
  * Replaces src/finite_volume/grp_solver_2D_EUL_source.c:75 (finite_volume.h:43-44). */
 void GRP_solver_2D_EUL_source(const int m, const int n, struct cell_var_stru *CV, double **X, double **Y,
@@ -129,6 +140,10 @@ int hydro2d_run(hydro2d_t *h, const double *cfg, int ncfg, int split, int stats,
  * initial specific total energy, or NULL to use the 1D driver's formula. */
 int hydro1d_run(int m, double *rho, double *u, double *p, double *E, const double *cfg, int ncfg, int order,
                 hydro_run_info *info);
+/* The Lagrangian schemes the same way; X (m+1 doubles, may be NULL) receives
+ * the final node coordinates, which start at j * cfg[10]. */
+int hydro1d_run_lag(int m, double *rho, double *u, double *p, double *E, double *X, const double *cfg, int ncfg,
+                    int order, hydro_run_info *info);
 /* Kernel variants of the unsplit step (tile shape / threads / occupancy).
  * hydro2d_get_variant fills shape[5] = {tile x, tile y, threads, min CTAs per SM,
  * shared-memory stages of the persistent TMA-staged kernel (1 or 2), 0 for one CTA per tile}. */

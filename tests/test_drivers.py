@@ -141,3 +141,41 @@ def test_2d_driver_binary_formats(gpu_lib, port, tmp_path, mode):
             assert not (out / f"{name}.dat").exists()
     _, _, xc = _read_bin(out / "X.bin")
     np.testing.assert_allclose(xc[0][0], (np.arange(m) + 0.5) / m, rtol=1e-14)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2])
+def test_1d_driver_lagrangian_sod(gpu_lib, tmp_path, order):
+    """hydrocode_1D.out ... LAG: the Lagrangian schemes through the driver;
+    output under data_out/one-dim/LAG_<order>_order, cell centres from the
+    moved nodes."""
+    exe = os.path.join(BUILD, "hydrocode_1D.out")
+    from hydro_gb300 import cases
+
+    rho, u, p = cases.sod(400)
+    case = tmp_path / "data_in" / "one-dim" / "SOD"
+    case.mkdir(parents=True)
+    for name, a in (("RHO", rho), ("U", u), ("P", p)):
+        (case / f"{name}.txt").write_text("\n".join(f"{x:.17g}" for x in a) + "\n")
+    (case / "config.txt").write_text("1 0.2\n4 1e-9\n5 100000\n6 1.4\n7 0.45\n10 0.0025\n17 -4\n")
+    run_dir = tmp_path / "src" / "hydrocode_1D"
+    run_dir.mkdir(parents=True)
+    r = subprocess.run([exe, "SOD", "sod_lag", str(order), "LAG"], cwd=run_dir, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Lagrangian scheme" in r.stdout
+    out = tmp_path / "data_out" / "one-dim" / f"LAG_{order}_order" / "sod_lag"
+    # the oracle with the device's correctly rounded pow: Sod-GRP in Lagrangian
+    # coordinates amplifies glibc's pow rounding to ~1e-8 in places (see
+    # test_parity_1d_lag.py), more than the text's 10 digits absorb
+    import oracle as orc
+
+    cfg = orc.default_config_1d(t_all=0.2, steps=100000, hx=0.0025, bx=-4, cfl=0.45)
+    want = orc.Oracle("crpow").run_1d_lag(rho, u, p, cfg, order)
+    for name, key in (("RHO", "rho"), ("U", "u"), ("P", "p")):
+        got = _read_dat(out / f"{name}.dat")
+        np.testing.assert_allclose(got[-1], want[key], rtol=RTOL_TEXT, atol=1e-12)
+    xc = _read_dat(out / "X.dat")
+    X = want["X"]
+    np.testing.assert_allclose(xc[-1], 0.5 * (X[1:] + X[:-1]), rtol=RTOL_TEXT, atol=1e-12)
+    np.testing.assert_allclose(xc[0], (np.arange(400) + 0.5) / 400, rtol=RTOL_TEXT)
