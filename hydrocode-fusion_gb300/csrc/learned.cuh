@@ -115,22 +115,6 @@ struct MlpShared {
     float b1[MLP_H], b2[MLP_H], b3;
 };
 
-// The shared-memory image built once in global memory (for kernels that read
-// the network through L1 instead of staging it in shared memory).
-static __global__ void k_mlp_image(const uint32_t* __restrict__ frag, const float* __restrict__ prm,
-                                   MlpShared* __restrict__ img)
-{
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    for (int q = tid; q < MLP_NFRAG; q += gridDim.x * blockDim.x)
-        img->frag[q] = frag[q];
-    if (tid < MLP_H) {
-        img->b1[tid] = prm[MLP_B1 + tid];
-        img->b2[tid] = prm[MLP_B2 + tid];
-    }
-    if (tid == 0)
-        img->b3 = prm[MLP_B3];
-}
-
 __device__ __forceinline__ void mlp_load_shared(MlpShared& S, const uint32_t* __restrict__ frag,
                                                 const float* __restrict__ prm, int tid, int nthreads)
 {
@@ -148,14 +132,18 @@ __device__ __forceinline__ float relu(float v) { return v > 0.f ? v : 0.f; }
 
 // Warp-cooperative forward pass: all 32 lanes call it with their own features
 // (garbage is fine for lanes that do not need the result); returns this lane's
-// output.
-__device__ __forceinline__ float warp_mlp(const float x[6], const MlpShared& S)
+// output.  rows (warp-uniform): only lanes below it need a result; with 16 or
+// fewer the second 16-row tile of the mma is skipped (its rows are independent
+// of the first's, so the results of lanes 0-15 do not change).
+__device__ __forceinline__ float warp_mlp(const float x[6], const MlpShared& S, int rows = 32)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     float mine = 0.f;
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
+        if (mt == 1 && rows <= 16)
+            break;
         // layer-1 A fragment: rows g and g+8 of this M tile, columns 2t and 2t+1 (6 and 7 are padding)
         const int s0 = mt * 16 + g, s1 = s0 + 8;
         float f0[6], f1[6];
@@ -220,10 +208,10 @@ __device__ __forceinline__ float warp_mlp(const float x[6], const MlpShared& S)
 // registers then do not add to the register pressure of the whole tile code
 // (the network runs on a small fraction of the faces).  All 32 lanes call it.
 static __device__ __noinline__ float warp_mlp_outline(float x0, float x1, float x2, float x3, float x4, float x5,
-                                                      const MlpShared* S)
+                                                      const MlpShared* S, int rows)
 {
     const float x[6] = {x0, x1, x2, x3, x4, x5};
-    return warp_mlp(x, *S);
+    return warp_mlp(x, *S, rows);
 }
 
 }  // namespace hydro

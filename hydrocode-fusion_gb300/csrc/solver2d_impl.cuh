@@ -375,8 +375,7 @@ public:
         variants = TS::all(form == HYDRO_FORM_FP32_LEARNED, rs);
         if (form == HYDRO_FORM_FP32_LEARNED) {
             if (!cuda_ok(cudaMalloc(&mlp_frag, sizeof(uint32_t) * MLP_NFRAG), "network") ||
-                !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network") ||
-                !cuda_ok(cudaMalloc(&mlp_img, sizeof(MlpShared)), "network"))
+                !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network"))
                 return -1;
         }
         int smem_optin = 0;
@@ -442,7 +441,6 @@ public:
 
     uint32_t* mlp_frag = nullptr;
     float* mlp_prm = nullptr;
-    MlpShared* mlp_img = nullptr;
     bool mlp_set = false;
 
     int set_mlp(const float* params) override
@@ -455,8 +453,7 @@ public:
                      "network upload"))
             return -1;
         k_mlp_pack<<<(8 * 32 + 4 * 8 * 32 + 4 * 32 + 127) / 128, 128, 0, stream>>>(mlp_prm, mlp_frag);
-        k_mlp_image<<<(MLP_NFRAG + 255) / 256, 256, 0, stream>>>(mlp_frag, mlp_prm, mlp_img);
-        count_launch(2);
+        count_launch(1);
         mlp_set = true;
         return cuda_ok(cudaStreamSynchronize(stream), "network pack") ? 0 : -1;
     }
@@ -466,7 +463,6 @@ public:
         if (stream) cudaStreamSynchronize(stream);
         cudaFree(mlp_frag);
         cudaFree(mlp_prm);
-        cudaFree(mlp_img);
         cudaFree(mem);
         cudaFree(ghost0);
         cudaFree(ctl);
@@ -700,7 +696,6 @@ public:
             }
             a.mlp_frag = mlp_frag;
             a.mlp_prm = mlp_prm;
-            a.mlp_img = mlp_img;
         }
 
         using TS = Variants<R>;

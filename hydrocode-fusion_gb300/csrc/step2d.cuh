@@ -77,7 +77,6 @@ struct StepArgs {
     int stats;             // count Newton faces / iterations
     const uint32_t* mlp_frag;  // learned form: packed BF16 network
     const float* mlp_prm;      // learned form: FP32 parameters (biases)
-    const MlpShared* mlp_img;  // learned form: the same image in global memory (read through L1)
 };
 
 // ---------------------------------------------------------------------------
@@ -271,11 +270,12 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
 }
 
 // Learned starting pressure of the exact solver for every lane of the warp
-// whose face is not a uniform pair (warp-collective: all 32 lanes call it).
-// Returns -1 where no guess applies (uniform pair, inactive lane, a pair that
-// would generate vacuum, a non-finite prediction).
+// whose face is not a uniform pair (warp-collective: all 32 lanes call it;
+// rows: only lanes below it are active).  Returns -1 where no guess applies
+// (uniform pair, inactive lane, a pair that would generate vacuum, a
+// non-finite prediction).
 __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<float>& Rr, bool active,
-                                               const Gas<float>& G, const MlpShared& M)
+                                               const Gas<float>& G, const MlpShared& M, int rows)
 {
     const float cL = sqrtf(G.g * L.p / L.rho), cR = sqrtf(G.g * Rr.p / Rr.rho);
     const float dist = sqrtf((L.rho - Rr.rho) * (L.rho - Rr.rho) + (L.u - Rr.u) * (L.u - Rr.u) +
@@ -289,7 +289,7 @@ __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<
 #pragma unroll
             for (int k = 0; k < 6; ++k)
                 x[k] = 0.f;
-        const float y = warp_mlp_outline(x[0], x[1], x[2], x[3], x[4], x[5], &M);
+        const float y = warp_mlp_outline(x[0], x[1], x[2], x[3], x[4], x[5], &M, rows);
         const bool vac = (Rr.u - L.u) >= 0.9f * 2.f * (cL + cR) / G.gm1;
         const float p = pbar * __expf(y);
         if (need && !vac && p > 0.f && p < INFINITY)
@@ -299,16 +299,16 @@ __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<
 }
 template <typename R>
 __device__ __forceinline__ R learned_guess_any(const Side<R>& L, const Side<R>& Rr, bool active, const Gas<R>& G,
-                                               const MlpShared& M);
+                                               const MlpShared& M, int rows);
 template <>
 __device__ __forceinline__ float learned_guess_any<float>(const Side<float>& L, const Side<float>& Rr, bool active,
-                                                          const Gas<float>& G, const MlpShared& M)
+                                                          const Gas<float>& G, const MlpShared& M, int rows)
 {
-    return learned_guess(L, Rr, active, G, M);
+    return learned_guess(L, Rr, active, G, M, rows);
 }
 template <>
 __device__ __forceinline__ double learned_guess_any<double>(const Side<double>&, const Side<double>&, bool,
-                                                            const Gas<double>&, const MlpShared&)
+                                                            const Gas<double>&, const MlpShared&, int)
 {
     return -1.0;
 }
@@ -327,9 +327,8 @@ struct UnsplitSmem {
     static constexpr int nQ = (TJ + 1) * TI + TJ * (TI + 1);  // queue of faces for the exact solver
     static constexpr size_t bytes_f = sizeof(R) * (size_t)(nW + nS + nFX + nFY);
     static constexpr size_t bytes = bytes_f + (2 * (size_t)nQ + 15) / 16 * 16;
-    // the learned form appends the starting pressures of the queued faces and the network image
-    static constexpr size_t p_off = (bytes + 15) / 16 * 16;
-    static constexpr size_t mlp_off = p_off + 4 * (size_t)nQ;
+    // the learned form appends the network image
+    static constexpr size_t mlp_off = (bytes + 15) / 16 * 16;
     static constexpr size_t bytes_learned = mlp_off + sizeof(MlpShared);
 };
 
@@ -362,8 +361,7 @@ template <typename R, int TJ, int TI, int NT, bool LEARNED, bool STAGED, int RS 
 __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
                                           R* __restrict__ W,
                                           const R* B, R* __restrict__ S, R* FX, R* __restrict__ FY,
-                                          unsigned short* __restrict__ Q, float* __restrict__ P,
-                                          const MlpShared& Mlp)
+                                          unsigned short* __restrict__ Q, const MlpShared& Mlp)
 {
     static_assert(!(LEARNED && RS != 0), "the learned start is built for the quasi-1D interface solver");
     using SM = UnsplitSmem<R, TJ, TI>;
@@ -618,32 +616,27 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
     }
     __syncthreads();
     // pass B: the queued faces, 32 per warp.  The learned form first runs the
-    // network over the whole queue (warp-collective, tensor cores) and keeps
-    // each face's starting pressure in P, so the network and the exact solver
-    // never hold their registers at the same time.
+    // network over the warp's 32 faces (warp-collective, tensor cores; one
+    // 16-row tile when no more than 16 are queued) and then solves them; the
+    // faces' sides are rebuilt after the network call, so the network and the
+    // exact solver never hold their registers at the same time.
     const int qn = s_qn;
-    if constexpr (LEARNED) {
-        for (int qb = tid - lane; qb < qn; qb += NT) {
-            const int q = qb + lane;
-            const bool act = q < qn;
+    for (int qb = tid - lane; qb < qn; qb += NT) {
+        const int q = qb + lane;
+        const bool act = q < qn;
+        R p_start = R(-1);
+        if constexpr (LEARNED) {
             Side<R> L, Rr;
             int lj = 0, li = 0, j = 0, i = 0;
             sides(act ? (int)Q[q] : 0, L, Rr, lj, li, j, i);
-            const R g = learned_guess_any<R>(L, Rr, act, G, Mlp);
-            if (act)
-                P[q] = (float)g;
+            p_start = learned_guess_any<R>(L, Rr, act, G, Mlp, qn - qb < 32 ? qn - qb : 32);
         }
-        __syncthreads();
-    }
-    for (int qb = tid - lane; qb < qn; qb += NT) {
-        const int q = qb + lane;
-        if (q >= qn)
+        if (!act)
             break;
         const int f = (int)Q[q];
         Side<R> L, Rr;
         int lj = 0, li = 0, j = 0, i = 0;
         sides(f, L, Rr, lj, li, j, i);
-        const R p_start = LEARNED ? (R)P[q] : R(-1);
         solve_store(std::integral_constant<int, 2>(), f, L, Rr, lj, li, j, i, p_start);
     }
     if (a.stats) {
@@ -751,8 +744,7 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const Gas<R>&
     R* FX = S + SM::nS;
     R* FY = FX + SM::nFX;
     unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + SM::bytes_f);
-    float* P = LEARNED ? reinterpret_cast<float*>(smem_raw + SM::p_off) : nullptr;
-    tile_body<R, TJ, TI, NT, LEARNED, false, RS>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, P, Mlp);
+    tile_body<R, TJ, TI, NT, LEARNED, false, RS>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, Mlp);
 }
 
 template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false, int RS = 0>
@@ -775,9 +767,9 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
 // the other stage, so global-memory latency overlaps the face solves within
 // the CTA; with STAGES = 1 the CTA waits for its own copy and the other CTAs
 // on the SM hide it (smaller shared memory, more CTAs per SM).
-//   shared memory: stage(s) | S | FY | face queue | [starting pressures] | 2 mbarriers
+//   shared memory: stage(s) | S | FY | face queue | [network image] | 2 mbarriers
 // (the x-fluxes FX reuse the slope box of the current stage, dead after the
-// limiter phase; the learned form reads its network from global memory).
+// limiter phase).
 // ---------------------------------------------------------------------------
 template <typename R, int TJ, int TI, bool LEARNED, int STAGES = 2>
 struct TmaSmem {
@@ -787,10 +779,10 @@ struct TmaSmem {
     static constexpr size_t s_off = STAGES * SL::bytes;
     static constexpr size_t fy_off = s_off + sizeof(R) * SM::nS;
     static constexpr size_t q_off = fy_off + sizeof(R) * SM::nFY;
-    static constexpr size_t p_off = (q_off + 2 * (size_t)SM::nQ + 15) / 16 * 16;
-    static constexpr size_t mlp_off = p_off + (LEARNED ? 4 * (size_t)SM::nQ : 0);
-    // the network stays in global memory here (a.mlp_img, cached in L1): shared memory is full
-    static constexpr size_t bar_off = (mlp_off + 15) / 16 * 16;
+    // the learned form keeps the network image here, loaded once per CTA (the
+    // persistent CTA serves many tiles; read through L1 it cost ~10% of a step)
+    static constexpr size_t mlp_off = (q_off + 2 * (size_t)SM::nQ + 15) / 16 * 16;
+    static constexpr size_t bar_off = (mlp_off + (LEARNED ? sizeof(MlpShared) : 0) + 15) / 16 * 16;
     static constexpr size_t bytes = bar_off + 16;
     // the dynamic shared memory follows the static variables, so its start is
     // only 16-byte aligned: 128 bytes of slack let the kernel align it itself
@@ -822,8 +814,9 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
     R* S = reinterpret_cast<R*>(smem_raw + TS::s_off);
     R* FY = reinterpret_cast<R*>(smem_raw + TS::fy_off);
     unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + TS::q_off);
-    float* P = LEARNED ? reinterpret_cast<float*>(smem_raw + TS::p_off) : nullptr;
-    const MlpShared& Mlp = *(LEARNED ? a.mlp_img : reinterpret_cast<const MlpShared*>(smem_raw));
+    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + TS::mlp_off);
+    if (LEARNED)  // made visible by the barrier after the mbarrier set-up below
+        mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + TS::bar_off);
     const int nti = (a.n + TI - 1) / TI;
     const int ntiles = nti * ((a.m + TJ - 1) / TJ);
@@ -874,8 +867,7 @@ __global__ void __launch_bounds__(NT, MINB) k_step_tma(const __grid_constant__ S
         unsigned char* cur = smem_raw + stg * SL::bytes;
         R* W = reinterpret_cast<R*>(cur + SL::a_off);
         R* B = reinterpret_cast<R*>(cur + SL::b_off);
-        tile_body<R, TJ, TI, NT, LEARNED, true, RS>(a, a.G, (t % nti) * TI, (t / nti) * TJ, W, B, S, B, FY, Q, P,
-                                                    Mlp);
+        tile_body<R, TJ, TI, NT, LEARNED, true, RS>(a, a.G, (t % nti) * TI, (t / nti) * TJ, W, B, S, B, FY, Q, Mlp);
     }
     if (failed && threadIdx.x == 0) {
         // let the copies still in flight land (bounded) before the CTA exits, then report
