@@ -215,6 +215,9 @@ def e2e_run(hg, state, m, n, K):
     rho, u, v, p = state
     cfg = hg.config_2d(t_all=-1, steps=K, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4, form=hg.FORM_FP32_LEARNED)
     c = Call2D(hg.lib(), rho, u, v, p, 1.4, cfg, N_MAX=2)
+    warm = Call2D(hg.lib(), rho, u, v, p, 1.4,
+                  hg.config_2d(t_all=-1, steps=3, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4, form=hg.FORM_FP32_LEARNED),
+                  N_MAX=2)
     # the scheme call reports on stdout as the reference's does: keep that
     # text out of this program's one JSON line
     import ctypes
@@ -223,6 +226,10 @@ def e2e_run(hg, state, m, n, K):
     saved, devnull = os.dup(1), os.open(os.devnull, os.O_WRONLY)
     os.dup2(devnull, 1)
     try:
+        # an untimed 3-step call first (the process's one-time costs: network
+        # file, driver entry points, kernel attributes); the timed call then
+        # still creates its solver, packs and copies the host arrays both ways
+        warm.call()
         l0 = hg.kernel_launches()
         t0 = time.perf_counter()
         nplot, k_out = c.call()
