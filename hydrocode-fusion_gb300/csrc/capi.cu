@@ -217,26 +217,53 @@ static Solver2DBase* make_solver(int m, int n, int form, int rs)
     }
 }
 
-// Runs fn(j0, j1) over row blocks of an m x n host copy on several host
-// threads when the copy is large (the caller's rows are separate allocations,
-// so the packing into and out of one buffer is plain memory traffic).
-template <typename F>
-static void parallel_rows(int m, int n, F fn)
+void parallel_range(int rows, size_t bytes, const std::function<void(int, int)>& fn)
 {
-    const size_t bytes = (size_t)m * n * 40;
     unsigned hw = std::thread::hardware_concurrency();
-    int T = bytes < (size_t)(64u << 20) ? 1 : (int)(hw ? (hw < 16 ? hw : 16) : 4);
-    if (T > m)
-        T = m;
+    int T = bytes < (size_t)(8u << 20) ? 1 : (int)(hw ? (hw < 16 ? hw : 16) : 4);
+    if (T > rows)
+        T = rows;
     if (T <= 1) {
-        fn(0, m);
+        fn(0, rows);
         return;
     }
     std::vector<std::thread> th;
-    for (int t = 0; t < T; ++t)
-        th.emplace_back([&, t] { fn((int)((long long)m * t / T), (int)((long long)m * (t + 1) / T)); });
+    for (int t = 1; t < T; ++t)
+        th.emplace_back([&, t] { fn((int)((long long)rows * t / T), (int)((long long)rows * (t + 1) / T)); });
+    fn(0, (int)((long long)rows / T));
     for (auto& x : th)
         x.join();
+}
+
+// Runs fn(j0, j1) over row blocks of an m x n host copy of the 5 state planes
+// (the caller's rows are separate allocations, so the packing into and out of
+// one buffer is plain memory traffic).
+template <typename F>
+static void parallel_rows(int m, int n, F fn)
+{
+    parallel_range(m, (size_t)m * n * 40, fn);
+}
+
+HostPair* host_pair()
+{
+    static HostPair* pp = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        HostPair* h = new HostPair();
+        h->bytes = (size_t)64 << 20;
+        for (int b = 0; b < 2; ++b) {
+            if (cudaHostAlloc(&h->buf[b], h->bytes, cudaHostAllocDefault) != cudaSuccess) {
+                cudaGetLastError();  // not pinned: the copies still work, staged by the driver
+                h->buf[b] = malloc(h->bytes);
+            }
+            if (cudaEventCreateWithFlags(&h->ev[b], cudaEventDisableTiming) != cudaSuccess || !h->buf[b]) {
+                set_error("host staging buffers");
+                return;
+            }
+        }
+        pp = h;
+    });
+    return pp;
 }
 
 // Shared body of the two 2D scheme entry points.
@@ -256,23 +283,8 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
     // gather and scatter those rows themselves; elsewhere the rows are packed
     // into one host buffer and copied.
     const bool direct = pageable_host_access();
-    std::vector<double> host(direct ? 0 : 5 * mn);
-    double* pl[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    if (!direct) {
-        for (int k = 0; k < 5; ++k)
-            pl[k] = &host[(size_t)k * mn];
-        parallel_rows(m, n, [&](int j0, int j1) {
-            for (int j = j0; j < j1; ++j) {
-                memcpy(pl[0] + (size_t)j * n, CV[0].RHO[j], n * sizeof(double));
-                memcpy(pl[1] + (size_t)j * n, CV[0].U[j], n * sizeof(double));
-                memcpy(pl[2] + (size_t)j * n, CV[0].V[j], n * sizeof(double));
-                memcpy(pl[3] + (size_t)j * n, CV[0].P[j], n * sizeof(double));
-                memcpy(pl[4] + (size_t)j * n, CV[0].E[j], n * sizeof(double));
-            }
-        });
-    }
     const double* const* in_rows[5] = {CV[0].RHO, CV[0].U, CV[0].V, CV[0].P, CV[0].E};
-    if (direct ? s->upload_rows(in_rows) : s->upload(pl[0], pl[1], pl[2], pl[3], pl[4], config[6])) {
+    if (direct ? s->upload_rows(in_rows) : s->upload_rows_staged(in_rows)) {
         fprintf(stderr, "hydro_gb300: upload failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }
@@ -290,7 +302,7 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
         exit(5);
     }
     double* const* out_rows[5] = {CV[nt].RHO, CV[nt].U, CV[nt].V, CV[nt].P, CV[nt].E};
-    if (direct ? s->download_rows(out_rows) : s->download(pl[0], pl[1], pl[2], pl[3], pl[4])) {
+    if (direct ? s->download_rows(out_rows) : s->download_rows_staged(out_rows)) {
         fprintf(stderr, "hydro_gb300: download failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }
@@ -308,8 +320,6 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
     };
     for (int k = 1; k < nt; ++k)  // CV[0] already holds the initial data
         scatter(k, snaps[k].data());
-    if (!direct)
-        scatter(nt, host.data());
 
     if (info.halted == 1)
         printf("Error on the time step %d (x-face code %d, y-face code %d); the step was discarded.\n", info.k_out,

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <functional>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -61,6 +63,12 @@ public:
     // device accesses pageable host memory coherently (pageable_host_access()).
     virtual int upload_rows(const double* const* const rows[5]) = 0;
     virtual int download_rows(double* const* const rows[5]) = 0;
+    // The same through the host staging pair (host_pair()): host threads pack
+    // a block of rows, converted to the state's precision, into one buffer
+    // while the previous block is copied from the other into the pitched
+    // state planes (and the reverse on the way out).
+    virtual int upload_rows_staged(const double* const* const rows[5]) = 0;
+    virtual int download_rows_staged(double* const* const rows[5]) = 0;
     // Runs the plan; snapshots (if any) are written as 5 x-major planes
     // (rho,u,v,p,E) each into snap_out[nt] (host memory, may be null).
     virtual int run(const RunConfig& rc, int split, int stats, const double* time_plot, int N_plot, int N_T,
@@ -83,6 +91,20 @@ Solver2DBase* make_solver2d_f32(int m, int n, int learned, int rs);
 // and writes pageable host memory coherently (Grace-Blackwell address
 // translation), so kernels may take the caller's malloc'd rows directly.
 bool pageable_host_access();
+
+// Two host buffers for the scheme entry points' row copies, pinned where the
+// driver grants it (else ordinary memory), kept for the life of the process;
+// the lock serialises their users.
+struct HostPair {
+    void* buf[2];
+    size_t bytes;
+    cudaEvent_t ev[2];
+    std::mutex lock;
+};
+HostPair* host_pair();
+// Runs fn(r0, r1) over [0, rows) on several host threads when the block is
+// large (bytes of host memory it touches).
+void parallel_range(int rows, size_t bytes, const std::function<void(int, int)>& fn);
 
 // error reporting + launch counting shared by all TUs
 void set_error(const std::string& msg);

@@ -369,7 +369,6 @@ public:
         if (!cuda_ok(cudaMemset(mem, 0, sizeof(R) * 26 * plane), "state clear")) return -1;
         if (!cuda_ok(cudaMalloc(&ghost0, sizeof(R) * (8 * (size_t)n + 8 * (size_t)m)), "ghost table")) return -1;
         if (!cuda_ok(cudaMalloc(&ctl, sizeof(Ctl)), "control block")) return -1;
-        if (!cuda_ok(cudaMalloc(&stage, sizeof(double) * 5 * (size_t)m * n), "staging")) return -1;
         if (!cuda_ok(cudaMalloc(&red, sizeof(unsigned long long)), "reduction")) return -1;
         using TS = Variants<R>;
         variants = TS::all(form == HYDRO_FORM_FP32_LEARNED, rs);
@@ -480,9 +479,19 @@ public:
         return (int)(b < cap ? (b ? b : 1) : cap);
     }
 
+    // FP64 staging of 5 planes for the host-plane API (upload/download and
+    // plot snapshots), allocated on first use: the scheme entry points copy
+    // rows through host buffers without it.
+    bool ensure_stage()
+    {
+        return stage || cuda_ok(cudaMalloc(&stage, sizeof(double) * 5 * (size_t)m * n), "staging");
+    }
+
     int upload(const double* rho, const double* u, const double* v, const double* p, const double* E,
                double gamma) override
     {
+        if (!ensure_stage())
+            return -1;
         size_t mn = (size_t)m * n;
         const double* src[4] = {rho, u, v, p};
         for (int k = 0; k < 4; ++k)
@@ -510,6 +519,8 @@ public:
 
     int download_planes(int b, double* const dst[5])
     {
+        if (!ensure_stage())
+            return -1;
         size_t mn = (size_t)m * n;
         for (int k = 0; k < 5; ++k) {
             if (!dst[k])
@@ -527,6 +538,109 @@ public:
     {
         double* dst[5] = {rho, u, v, p, E};
         return download_planes(cur_w, dst);
+    }
+
+    // A host value in the state's precision, rounded as the FP32 forms' device
+    // conversion rounds it (to nearest, a subnormal float result flushed to a
+    // zero of its sign: those kernels are compiled with --use_fast_math).
+    static R to_state(double x)
+    {
+        if constexpr (sizeof(R) == 4) {
+            float f = (float)x;
+            if (f != 0.f && fabsf(f) < 1.17549435e-38f)
+                f = copysignf(0.f, f);
+            return f;
+        } else {
+            return x;
+        }
+    }
+
+    int upload_rows_staged(const double* const* const rows[5]) override
+    {
+        HostPair* hp = host_pair();
+        if (!hp)
+            return -1;
+        std::lock_guard<std::mutex> guard(hp->lock);
+        const size_t row_bytes = sizeof(R) * (size_t)n;
+        const int CH = (int)(hp->bytes / row_bytes > 0 ? (hp->bytes / row_bytes < (size_t)m ? hp->bytes / row_bytes : m) : 1);
+        bool used[2] = {false, false};
+        int b = 0;
+        for (int k = 0; k < 5; ++k)
+            for (int j0 = 0; j0 < m; j0 += CH) {
+                const int j1 = j0 + CH < m ? j0 + CH : m;
+                // the copy that last read this buffer is done before it is refilled
+                if (used[b] && !cuda_ok(cudaEventSynchronize(hp->ev[b]), "staging wait"))
+                    return -1;
+                R* dst = static_cast<R*>(hp->buf[b]);
+                const double* const* src = rows[k];
+                parallel_range(j1 - j0, (size_t)(j1 - j0) * n * (8 + sizeof(R)), [&](int r0, int r1) {
+                    for (int r = r0; r < r1; ++r) {
+                        const double* sr = src[j0 + r];
+                        R* dr = dst + (size_t)r * n;
+                        if constexpr (sizeof(R) == 8) {
+                            memcpy(dr, sr, row_bytes);
+                        } else {
+                            for (int i = 0; i < n; ++i)
+                                dr[i] = to_state(sr[i]);
+                        }
+                    }
+                });
+                if (!cuda_ok(cudaMemcpy2DAsync(W(0) + k * plane + (size_t)j0 * ld, sizeof(R) * ld, dst, row_bytes,
+                                               row_bytes, j1 - j0, cudaMemcpyHostToDevice, stream),
+                             "upload") ||
+                    !cuda_ok(cudaEventRecord(hp->ev[b], stream), "staging event"))
+                    return -1;
+                used[b] = true;
+                b ^= 1;
+            }
+        // slopes start at zero (the first limiting uses minmod2 and ignores them)
+        if (!cuda_ok(cudaMemsetAsync(Sx(0), 0, sizeof(R) * 8 * plane, stream), "clear")) return -1;
+        if (!cuda_ok(cudaMemsetAsync(Sx(1), 0, sizeof(R) * 8 * plane, stream), "clear")) return -1;
+        cur_w = cur_s = cur_t = 0;
+        return cuda_ok(cudaStreamSynchronize(stream), "upload sync") ? 0 : -1;
+    }
+
+    int download_rows_staged(double* const* const rows[5]) override
+    {
+        HostPair* hp = host_pair();
+        if (!hp)
+            return -1;
+        std::lock_guard<std::mutex> guard(hp->lock);
+        const size_t row_bytes = sizeof(R) * (size_t)n;
+        const int CH = (int)(hp->bytes / row_bytes > 0 ? (hp->bytes / row_bytes < (size_t)m ? hp->bytes / row_bytes : m) : 1);
+        const int per_plane = (m + CH - 1) / CH, nchunk = 5 * per_plane;
+        auto issue = [&](int c) -> bool {
+            const int k = c / per_plane, j0 = (c % per_plane) * CH, j1 = j0 + CH < m ? j0 + CH : m, bb = c & 1;
+            return cuda_ok(cudaMemcpy2DAsync(hp->buf[bb], row_bytes, W(cur_w) + k * plane + (size_t)j0 * ld,
+                                             sizeof(R) * ld, row_bytes, j1 - j0, cudaMemcpyDeviceToHost, stream),
+                           "download") &&
+                   cuda_ok(cudaEventRecord(hp->ev[bb], stream), "staging event");
+        };
+        if (!issue(0))
+            return -1;
+        for (int c = 0; c < nchunk; ++c) {
+            // the next block's copy runs while this one is unpacked (its buffer was emptied last turn)
+            if (c + 1 < nchunk && !issue(c + 1))
+                return -1;
+            if (!cuda_ok(cudaEventSynchronize(hp->ev[c & 1]), "download wait"))
+                return -1;
+            const int k = c / per_plane, j0 = (c % per_plane) * CH, j1 = j0 + CH < m ? j0 + CH : m;
+            const R* srcb = static_cast<const R*>(hp->buf[c & 1]);
+            double* const* dst = rows[k];
+            parallel_range(j1 - j0, (size_t)(j1 - j0) * n * (8 + sizeof(R)), [&](int r0, int r1) {
+                for (int r = r0; r < r1; ++r) {
+                    const R* sr = srcb + (size_t)r * n;
+                    double* dr = dst[j0 + r];
+                    if constexpr (sizeof(R) == 8) {
+                        memcpy(dr, sr, row_bytes);
+                    } else {
+                        for (int i = 0; i < n; ++i)
+                            dr[i] = (double)sr[i];
+                    }
+                }
+            });
+        }
+        return 0;
     }
 
     int upload_rows(const double* const* const rows[5]) override

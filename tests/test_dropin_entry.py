@@ -69,3 +69,34 @@ def test_1d_entry_sod(gpu_lib, order):
     assert nplot == 2 and k_out == d[f"sod{order}/meta"][0] and time_plot[1] == d[f"sod{order}/meta"][1]
     for f, key in enumerate(("rho", "u", "p", "E")):
         assert rel_l1(data[f, 1], d[f"sod{order}/{key}"]) <= TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1, 2])
+def test_entry_row_copies_match_plane_api(gpu_lib, form, monkeypatch):
+    """The scheme call's staged row copies (host threads pack the caller's
+    rows, converted to the form's precision, through a pair of host buffers)
+    and the plane API (the device converts) leave the same state bit for bit,
+    values at and below the float subnormal range included."""
+    monkeypatch.delenv("HYDRO_DIRECT_HOST_ROWS", raising=False)
+    hg = gpu_lib
+    from hydro_gb300 import cases
+
+    m, n = 40, 33
+    rho, u, v, p = (a.copy() for a in cases.four_quadrant(m, n, 6))
+    u[3, 4], u[5, 6], v[7, 8], v[9, 10] = 1e-40, -3e-39, 1.1754942e-38, 5e-324
+    cfg = hg.config_2d(t_all=-1, steps=15, hx=1 / m, hy=1 / n, bx=-4, by=-4, form=form)
+    data, nplot, _, _ = call_2d(hg.lib(), rho, u, v, p, 1.4, cfg.copy())
+    E = 0.5 * u * u + p / (1.4 - 1.0) / rho
+    E += 0.5 * v * v  # the driver's energy, as the scheme call receives it
+    s = hg.Solver2D(m, n, form)
+    try:
+        if form == hg.FORM_FP32_LEARNED:
+            s.set_mlp(hg.load_weights())
+        s.upload(rho, u, v, p, E)
+        s.run(cfg)
+        want = s.download()
+    finally:
+        s.close()
+    for f, key in enumerate(("rho", "u", "v", "p", "E")):
+        assert np.array_equal(data[nplot - 1, f], want[key]), key
