@@ -141,6 +141,25 @@ def cpu_rate(m, n, steps, threads):
     return m * n * steps / out["wall"], out["wall"]
 
 
+def slowest_rank_ms(ms, dist, device):
+    """The job's time over ranks: the maximum (every rank advances its own
+    grid, and the job ends when the slowest replica does); ms itself with one
+    rank."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(cells, steps, ms, world):
+    """Whole-job cell-updates/s of `world` replicas that each advance `cells`
+    cells `steps` steps, the slowest taking ms milliseconds."""
+    return world * cells * steps / (ms * 1e-3)
+
+
 def rel_l1(a, b):
     d = np.abs(b).sum()
     return float(np.abs(a - b).sum() / d) if d > 0 else float(np.abs(a - b).sum())
@@ -181,11 +200,7 @@ def timed_form(hg, form, state, m, n, K, W, tune, stats_steps, clocks=False, dis
             sampler.__exit__(None, None, None)
         torch.cuda.synchronize()
         res["launches"] = hg.kernel_launches() - l0
-        ms = info.gpu_ms
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = slowest_rank_ms(info.gpu_ms, dist, "cuda")
         res["gpu_ms"] = ms
         res["ms_per_step"] = ms / K
         res["value"] = m * n * K / (ms * 1e-3)
@@ -395,7 +410,7 @@ def main():
     head = timed_form(hg, hg.FORM_FP32_LEARNED, state, m, n, K, W, tune, args.stats_steps, clocks=True, dist=dist)
     if dist is not None:
         dist.barrier()
-    value = world * head["value"]  # replicas: every rank advances its own grid
+    value = replicas_value(m * n, K, head["gpu_ms"], world)  # replicas: every rank advances its own grid
     if rank != 0:
         return
     plain = timed_form(hg, hg.FORM_FP32, state, m, n, K, W, tune, args.stats_steps)
