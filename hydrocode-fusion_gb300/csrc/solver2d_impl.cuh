@@ -517,21 +517,21 @@ public:
         return cuda_ok(cudaStreamSynchronize(stream), "upload sync") ? 0 : -1;
     }
 
+    // State buffer b into x-major FP64 planes (dst[k] may be null), through
+    // the host staging pair like the scheme entry points' rows.
     int download_planes(int b, double* const dst[5])
     {
-        if (!ensure_stage())
-            return -1;
-        size_t mn = (size_t)m * n;
+        std::vector<double*> ptr(5 * (size_t)m);
+        double* const* rows[5];
         for (int k = 0; k < 5; ++k) {
+            rows[k] = nullptr;
             if (!dst[k])
                 continue;
-            k_unpack_plane<R><<<grid1d(mn), 256, 0, stream>>>(W(b) + k * plane, stage + k * mn, m, n, ld);
-            count_launch();
-            if (!cuda_ok(cudaMemcpyAsync(dst[k], stage + k * mn, sizeof(double) * mn, cudaMemcpyDeviceToHost, stream),
-                         "download"))
-                return -1;
+            for (int j = 0; j < m; ++j)
+                ptr[(size_t)k * m + j] = dst[k] + (size_t)j * n;
+            rows[k] = &ptr[(size_t)k * m];
         }
-        return cuda_ok(cudaStreamSynchronize(stream), "download sync") ? 0 : -1;
+        return download_rows_staged_from(b, rows);
     }
 
     int download(double* rho, double* u, double* v, double* p, double* E) override
@@ -600,7 +600,10 @@ public:
         return cuda_ok(cudaStreamSynchronize(stream), "upload sync") ? 0 : -1;
     }
 
-    int download_rows_staged(double* const* const rows[5]) override
+    int download_rows_staged(double* const* const rows[5]) override { return download_rows_staged_from(cur_w, rows); }
+
+    // State buffer b into the caller's rows (rows[k] may be null: plane k is skipped).
+    int download_rows_staged_from(int b, double* const* const rows[5])
     {
         HostPair* hp = host_pair();
         if (!hp)
@@ -608,14 +611,22 @@ public:
         std::lock_guard<std::mutex> guard(hp->lock);
         const size_t row_bytes = sizeof(R) * (size_t)n;
         const int CH = (int)(hp->bytes / row_bytes > 0 ? (hp->bytes / row_bytes < (size_t)m ? hp->bytes / row_bytes : m) : 1);
-        const int per_plane = (m + CH - 1) / CH, nchunk = 5 * per_plane;
+        // the chunks to copy: (plane, first row), planes the caller asked for
+        std::vector<std::pair<int, int>> ch;
+        for (int k = 0; k < 5; ++k)
+            if (rows[k])
+                for (int j0 = 0; j0 < m; j0 += CH)
+                    ch.push_back({k, j0});
+        const int nchunk = (int)ch.size();
         auto issue = [&](int c) -> bool {
-            const int k = c / per_plane, j0 = (c % per_plane) * CH, j1 = j0 + CH < m ? j0 + CH : m, bb = c & 1;
-            return cuda_ok(cudaMemcpy2DAsync(hp->buf[bb], row_bytes, W(cur_w) + k * plane + (size_t)j0 * ld,
+            const int k = ch[c].first, j0 = ch[c].second, j1 = j0 + CH < m ? j0 + CH : m, bb = c & 1;
+            return cuda_ok(cudaMemcpy2DAsync(hp->buf[bb], row_bytes, W(b) + k * plane + (size_t)j0 * ld,
                                              sizeof(R) * ld, row_bytes, j1 - j0, cudaMemcpyDeviceToHost, stream),
                            "download") &&
                    cuda_ok(cudaEventRecord(hp->ev[bb], stream), "staging event");
         };
+        if (nchunk == 0)
+            return 0;
         if (!issue(0))
             return -1;
         for (int c = 0; c < nchunk; ++c) {
@@ -624,7 +635,7 @@ public:
                 return -1;
             if (!cuda_ok(cudaEventSynchronize(hp->ev[c & 1]), "download wait"))
                 return -1;
-            const int k = c / per_plane, j0 = (c % per_plane) * CH, j1 = j0 + CH < m ? j0 + CH : m;
+            const int k = ch[c].first, j0 = ch[c].second, j1 = j0 + CH < m ? j0 + CH : m;
             const R* srcb = static_cast<const R*>(hp->buf[c & 1]);
             double* const* dst = rows[k];
             parallel_range(j1 - j0, (size_t)(j1 - j0) * n * (8 + sizeof(R)), [&](int r0, int r1) {
