@@ -344,6 +344,77 @@ def g2d_suite(hg, state, m, n, K, K64, W, tune, stats_steps):
     return out
 
 
+MF_BYTES_PER_FACE = 40 * 8 + 18 * 8 + 4   # fields in, fluxes out, status
+
+
+def mf_faces(rng, n):
+    """Two-component faces (field-major, 40 x n): a gamma per side in
+    [1.1, 3], densities and pressures log-uniform over e^-2..e^2, velocities
+    uniform, unit-normal slopes, volume/mass fractions in [0, 1], any normal;
+    a fifth of the faces are uniform pairs (the acoustic case)."""
+    f = np.empty((40, n))
+    th = rng.uniform(0, 2 * np.pi, n)
+    f[0], f[1] = np.cos(th), np.sin(th)
+    for b in (2, 21):
+        f[b] = rng.uniform(1.1, 3.0, n)
+        f[b + 1] = np.exp(rng.uniform(-2, 2, n))
+        f[b + 2:b + 4] = rng.uniform(-2, 2, (2, n))
+        f[b + 4] = np.exp(rng.uniform(-2, 2, n))
+        f[b + 5:b + 13] = rng.normal(0, 1, (8, n))
+        f[b + 13] = rng.uniform(0, 1, n)
+        f[b + 14:b + 16] = rng.normal(0, 1, (2, n))
+        f[b + 16] = rng.uniform(0, 1, n)
+        f[b + 17:b + 19] = rng.normal(0, 1, (2, n))
+    k = n // 5
+    f[22:26, :k] = f[3:7, :k]
+    return f
+
+
+def mf_suite(hg, peak, nface=8 << 20, reps=5, cpu=True):
+    """The two-component interface flux (GRP_2D_flux, MULTIFLUID_BASICS) on a
+    batch of nface faces through hydro_grp2d_flux_mf: kernel time (inputs in
+    HBM), the call's wall time with the host copies, and the oracle's serial
+    loop on a sample."""
+    rng = np.random.default_rng(2025)
+    base = mf_faces(rng, 1 << 20)
+    f = np.tile(base, (1, nface >> 20))
+    cfg = np.full(400, np.inf)
+    cfg[4], cfg[6], cfg[60], cfg[106] = 1e-9, 1.4, 1.0, 3.0
+    tau = 1e-4
+    hg.grp2d_flux_mf(f, tau, cfg)   # warm-up: buffers, module load
+    kern, wall = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out, status, info = hg.grp2d_flux_mf(f, tau, cfg)
+        wall.append(time.perf_counter() - t0)
+        kern.append(info.kernel_ms)
+    k_ms = float(np.median(kern))
+    w_s = float(np.median(wall))
+    res = {"workload": f"{nface} two-component faces (seeded, a fifth uniform pairs), gamma_a 1.4, gamma_b 3.0",
+           "value": nface / (k_ms * 1e-3), "unit": "faces/s", "kernel_ms": k_ms,
+           "e2e": {"value": nface / w_s, "unit": "faces/s", "wall_ms": w_s * 1e3,
+                   "h2d_bytes": 40 * 8 * nface, "d2h_bytes": (18 * 8 + 4) * nface},
+           "hbm": {"bytes_per_face": MF_BYTES_PER_FACE,
+                   "achieved_gbs": MF_BYTES_PER_FACE * nface / (k_ms * 1e-3) / 1e9, "peak_gbs": peak},
+           "bad_faces": int(info.n_bad), "resumed_faces": [int(info.resumed[0]), int(info.resumed[1])]}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        sample = 1 << 17
+        idx = np.arange(sample) * (nface // sample)      # spread over the batch's mix of cases
+        rows = np.ascontiguousarray(f[:, idx].T)
+        port = orc.Oracle("port")
+        t0 = time.perf_counter()
+        want = port.grp2d_flux_mf(rows, tau, 1e-9, 1.4, 3.0, True)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": sample / dt, "unit": "faces/s", "cores": 1, "kind": "port",
+                               "sample": f"{sample} faces spread over the batch, the oracle's serial loop"}
+        ok = want[:, 18] == 0
+        res["rel_l1_vs_oracle_sample"] = float(np.abs(out[:, idx].T[ok] - want[ok, :18]).sum() /
+                                               np.abs(want[ok, :18]).sum())
+    return res
+
+
 def reference_arm(args, m, n, rank):
     if rank != 0:
         return
@@ -380,6 +451,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-shear", action="store_true")
     ap.add_argument("--no-g2d", action="store_true")
+    ap.add_argument("--no-mf", action="store_true")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=300)
     args = ap.parse_args()
@@ -454,6 +526,7 @@ def main():
     batch = None if args.no_batch else batch_run(hg, args.batch_count, args.batch_steps, 5, 8)
     shear = None if args.no_shear else shear_suite(hg, m, n, K, W, tune, args.stats_steps)
     g2d = None if args.no_g2d else g2d_suite(hg, state, m, n, K, k64, W, tune, args.stats_steps)
+    mf = None if args.no_mf else mf_suite(hg, peak, cpu=not args.no_cpu)
 
     cpu = None
     if not args.no_cpu:
@@ -469,7 +542,8 @@ def main():
                        "grid": [m, n], "parallelism": "replicas" if world > 1 else "single",
                        "l2": "no flush: 13 planes x 4 B x 16.8M cells = 872 MB per state >> 129 MB L2"},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "gpu_launches": int(head["launches"]),
-            "clocks": head["clocks"], "forms": forms, "shear": shear, "g2d": g2d, "batch": batch}
+            "clocks": head["clocks"], "forms": forms, "shear": shear, "g2d": g2d, "batch": batch,
+            "mf_flux": mf}
     print(json.dumps(line), flush=True)
 
 

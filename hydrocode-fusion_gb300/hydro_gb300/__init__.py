@@ -69,6 +69,20 @@ class BatchInfo(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class FaceInfo(ctypes.Structure):
+    """hydro_face_info: outcome of one hydro_grp2d_flux_mf call."""
+    _fields_ = [
+        ("n_bad", ctypes.c_int),
+        ("first_bad", ctypes.c_int),
+        ("first_code", ctypes.c_int),
+        ("resumed", ctypes.c_int * 2),
+        ("kernel_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 SCHEDULES = ("persistent-static", "persistent-static-largest-first", "persistent-dynamic",
              "persistent-dynamic-largest-first", "graph-per-step")
 
@@ -133,6 +147,9 @@ def lib() -> ctypes.CDLL:
     L.hydro_batch_autotune.argtypes = [vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
     L.hydro_batch_problem_info.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    L.hydro_grp2d_flux_mf.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_double,
+                                      ctypes.POINTER(FaceInfo)]
+    L.hydro_grp2d_flux_mf.restype = ctypes.c_int
     L.hydro_gb300_last_error.restype = ctypes.c_char_p
     L.hydro_gb300_kernel_launches.restype = ctypes.c_ulonglong
     _lib = L
@@ -272,6 +289,34 @@ def run_2d(rho, u, v, p, cfg, split=False, form=FORM_FP64, stats=False, mlp=None
         return s.download(), info
     finally:
         s.close()
+
+
+# Field order of the two-component face batch (hydro_grp2d_flux_mf).
+MF_SIDE_FIELDS = ("gamma", "rho", "u", "v", "p", "d_rho", "d_u", "d_v", "d_p", "t_rho", "t_u", "t_v", "t_p",
+                  "z", "d_z", "t_z", "phi", "d_phi", "t_phi")
+MF_OUT_FIELDS = ("F_rho", "F_u", "F_v", "F_e", "RHO_int", "U_int", "V_int", "P_int", "F_phi", "F_gamma", "F_e_a",
+                 "PHI", "Z_a", "U_qt_add_c", "V_qt_add_c", "U_qt_star", "V_qt_star", "P_star")
+
+
+def grp2d_flux_mf(fields, tau, cfg):
+    """Two-component GRP_2D_flux for a batch of faces on the GPU.
+    fields: (40, nface) float64 -- n_x, n_y, then MF_SIDE_FIELDS for the left
+    and the right side.  cfg: config[] (4 eps, 6 / 106 the two gammas, 60
+    store F_gamma).  Returns (out (18, nface) in MF_OUT_FIELDS order,
+    status (nface,) int32, FaceInfo)."""
+    fields = np.ascontiguousarray(fields, np.float64)
+    if fields.ndim != 2 or fields.shape[0] != 40:
+        raise ValueError("fields must have shape (40, nface)")
+    nface = fields.shape[1]
+    out = np.zeros((18, nface))
+    status = np.zeros(nface, np.int32)
+    cfg = np.ascontiguousarray(cfg, np.float64)
+    info = FaceInfo()
+    rc = lib().hydro_grp2d_flux_mf(nface, fields, out, status.ctypes.data_as(ctypes.c_void_p), cfg, len(cfg),
+                                   float(tau), ctypes.byref(info))
+    if rc != 0:
+        raise RuntimeError("hydro_grp2d_flux_mf failed: " + last_error())
+    return out, status, info
 
 
 class Mlp:

@@ -262,6 +262,35 @@ typedef struct {
 } hydro_batch_opts;
 int hydro_gb300_batch_run(hydro_problem *probs, int nprob, int steps, hydro_batch_opts *o);
 
+/* ---- two-component interface flux (MULTIFLUID_BASICS) --------------------
+ * Replaces GRP_2D_flux of the reference's two-component build
+ * (src/flux_calc/flux_solver.c:158-237 with MULTIFLUID_BASICS; struct i_f_var,
+ * src/include/var_struc.h:116-142) for a batch of nface independent faces.
+ * in:  [40][nface] host array, field k of face f at in[k*nface + f]:
+ *      0 n_x, 1 n_y; left side from 2, right side from 21, each 19 fields:
+ *      gamma, RHO, U, V, P, d_rho, d_u, d_v, d_p, t_rho, t_u, t_v, t_p,
+ *      Z_a, d_z_a, t_z_a, PHI, d_phi, t_phi.
+ * out: [18][nface]: F_rho, F_u, F_v, F_e, RHO_int, U_int, V_int, P_int, F_phi,
+ *      F_gamma, F_e_a, PHI, Z_a, U_qt_add_c, V_qt_add_c, U_qt_star, V_qt_star, P_star
+ *      (the members GRP_2D_flux writes into the left struct).
+ * status: [nface] GRP_2D_flux's return value (star_dire_check: 1 non-positive
+ *      density or pressure, 2 non-finite t-axis value, 3 non-finite derivative).
+ *      Unlike the reference, which returns before writing the fluxes of such
+ *      a face, the outputs are written for every face.
+ * cfg: the reference's config[] (4 eps, 6 gamma of fluid a, 60 store F_gamma,
+ *      106 gamma of fluid b; entries at or beyond ncfg read as INFINITY, the
+ *      reference's default).  tau: the time step.
+ * Returns 0, -1 on a CUDA error, -2 on bad arguments. */
+typedef struct {
+    int n_bad;          /* faces with a non-zero status */
+    int first_bad;      /* smallest such face index, -1 if none */
+    int first_code;     /* its status */
+    int resumed[2];     /* faces whose Newton iteration went on in the second / third pass */
+    double kernel_ms;   /* device time of the flux kernels */
+} hydro_face_info;
+int hydro_grp2d_flux_mf(int nface, const double *in, double *out, int *status, const double *cfg, int ncfg,
+                        double tau, hydro_face_info *info);
+
 /* Number of CUDA kernels launched by this library since load (all solvers). */
 unsigned long long hydro_gb300_kernel_launches(void);
 /* Message of the last failing call in this thread ("" if none). */

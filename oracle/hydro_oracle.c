@@ -39,6 +39,15 @@ typedef struct {
     double trho, tu, tv, tp; /* tangential derivatives                    */
 } orc_side;
 
+/* Passive scalars of the two-component build (MULTIFLUID_BASICS): volume
+ * fraction z and mass fraction phi of one side, each with its normal and
+ * tangential derivative (struct i_f_var Z_a/d_z_a/t_z_a, PHI/d_phi/t_phi,
+ * src/include/var_struc.h:129-130). */
+typedef struct {
+    double z, dz, tz;
+    double phi, dphi, tphi;
+} orc_scal;
+
 /* Ghost cell of one boundary row/column, same fields as the reference's
  * struct b_f_var (src/include/var_struc.h:146-151). */
 typedef struct {
@@ -226,10 +235,37 @@ typedef struct {
 static void orc_g2d_nonacoustic(double gL, double gR, const orc_side *Ls, const orc_side *Rs, double eps,
                                 const orc_star *st, double D[4], double U[4]);
 
+/* The scalars' t-axis values UX = (z, phi) and derivatives DX when taken from
+ * one side's states as they stand (the states left/right of all waves):
+ * linear_grp_solver_Edir_Q1D.c:147-154, 162-169, 264-271, 279-286. */
+static void orc_scal_side(const orc_scal *X, double u, double v, double lu, double lv, double DX[2], double UX[2])
+{
+    UX[0] = X->z;
+    UX[1] = X->phi;
+    DX[0] = -(u - lu) * X->dz - (v - lv) * X->tz;
+    DX[1] = -(u - lu) * X->dphi - (v - lv) * X->tphi;
+}
+
+/* Scalars: XL/XR the two sides' (z, phi) with derivatives, DX/UX their outputs;
+ * all NULL for the single-fluid build (the reference's constant slots). */
+static void orc_q1d_solve_x(double gL, double gR, const orc_side *Ls, const orc_side *Rs,
+                            const orc_scal *XL, const orc_scal *XR,
+                            double eps, double atc, double ws[2], double D[4], double U[4], double S[4],
+                            double DX[2], double UX[2], int *newton_iters, int g2d);
+
 static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_side *Rs,
                           double eps, double atc, double ws[2], double D[4], double U[4], double S[4],
                           int *newton_iters, int g2d)
 {
+    orc_q1d_solve_x(gL, gR, Ls, Rs, NULL, NULL, eps, atc, ws, D, U, S, NULL, NULL, newton_iters, g2d);
+}
+
+static void orc_q1d_solve_x(double gL, double gR, const orc_side *Ls, const orc_side *Rs,
+                            const orc_scal *XL, const orc_scal *XR,
+                            double eps, double atc, double ws[2], double D[4], double U[4], double S[4],
+                            double DX[2], double UX[2], int *newton_iters, int g2d)
+{
+    const int sc = XL != NULL;
     const double lu = 0.0, lv = 0.0;
     const double rho_L = Ls->rho, rho_R = Rs->rho;
     const double d_rho_L = Ls->drho, d_rho_R = Rs->drho;
@@ -311,12 +347,16 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
             D[1] = -(u_L - lu) * d_u_L - (v_L - lv) * t_u_L - d_p_L / rho_L;
             D[2] = -(u_L - lu) * d_v_L - (v_L - lv) * t_v_L - t_p_L / rho_L;
             D[3] = -(u_L - lu) * d_p_L - (v_L - lv) * t_p_L - rho_L * c_L * c_L * (d_u_L + t_v_L);
+            if (sc)
+                orc_scal_side(XL, u_L, v_L, lu, lv, DX, UX);
         } else if (speed_R < lu) {
             U[0] = rho_R; U[1] = u_R; U[2] = v_R; U[3] = p_R;
             D[0] = -(u_R - lu) * d_rho_R - (v_R - lv) * t_rho_R - rho_R * (d_u_R + t_v_R);
             D[1] = -(u_R - lu) * d_u_R - (v_R - lv) * t_u_R - d_p_R / rho_R;
             D[2] = -(u_R - lu) * d_v_R - (v_R - lv) * t_v_R - t_p_R / rho_R;
             D[3] = -(u_R - lu) * d_p_R - (v_R - lv) * t_p_R - rho_R * c_R * c_R * (d_u_R + t_v_R);
+            if (sc)
+                orc_scal_side(XR, u_R, v_R, lu, lv, DX, UX);
         } else {
             if (CRW[0] && ((u_star - c_star_L) > lu)) {
                 U[1] = zetaL * (u_L + 2.0 * (c_L + lu) / (gL - 1.0));
@@ -356,6 +396,16 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
             D[1] = -(U[1] - lu) * D_u - (U[2] - lv) * T_u - D_p / U[0];
             D[2] = -(U[1] - lu) * D_v - (U[2] - lv) * T_v - T_p / U[0];
             D[3] = -(U[1] - lu) * D_p - (U[2] - lv) * T_p - U[0] * C * C * (D_u + T_v);
+            if (sc) { /* :180-210 (the side of the t-axis state), :220-245 */
+                const orc_scal *Xu = (CRW[0] && ((u_star - c_star_L) > lu)) ? XL
+                                   : (CRW[1] && ((u_star + c_star_R) < lu)) ? XR
+                                   : (u_star > lu) ? XL : XR;
+                const orc_scal *Xd = (u_star > lu) ? XL : XR;
+                UX[0] = Xu->z;
+                UX[1] = Xu->phi;
+                DX[0] = -(U[1] - lu) * Xd->dz - (U[2] - lv) * Xd->tz;
+                DX[1] = -(U[1] - lu) * Xd->dphi - (U[2] - lv) * Xd->tphi;
+            }
         }
         return;
     }
@@ -374,6 +424,8 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
         D[1] = -(u_L - lu) * d_u_L - (v_L - lv) * t_u_L - d_p_L / rho_L;
         D[2] = -(u_L - lu) * d_v_L - (v_L - lv) * t_v_L - t_p_L / rho_L;
         D[3] = -(u_L - lu) * d_p_L - (v_L - lv) * t_p_L - rho_L * c_L * c_L * (d_u_L + t_v_L);
+        if (sc)
+            orc_scal_side(XL, u_L, v_L, lu, lv, DX, UX);
         return;
     }
     if (speed_R < lu) {
@@ -382,6 +434,8 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
         D[1] = -(u_R - lu) * d_u_R - (v_R - lv) * t_u_R - d_p_R / rho_R;
         D[2] = -(u_R - lu) * d_v_R - (v_R - lv) * t_v_R - t_p_R / rho_R;
         D[3] = -(u_R - lu) * d_p_R - (v_R - lv) * t_p_R - rho_R * c_R * c_R * (d_u_R + t_v_R);
+        if (sc)
+            orc_scal_side(XR, u_R, v_R, lu, lv, DX, UX);
         return;
     }
     if (CRW[0] && ((u_star - c_star_L) > lu)) { /* sonic point in the 1-rarefaction, :290-314 */
@@ -400,6 +454,12 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
         D[0] = U[0] * (U[1] - lu) * pow(c_frac, (1.0 + zetaL) / zetaL) * TdS * (gL - 1.0);
         D[0] = (D[0] + D[3]) / C / C;
         D[2] = -(U[1] - lu) * d_v_L * U[0] / rho_L;
+        if (sc) {
+            UX[0] = XL->z;
+            UX[1] = XL->phi;
+            DX[0] = -(U[1] - lu) * XL->dz * U[0] / rho_L;
+            DX[1] = -(U[1] - lu) * XL->dphi * U[0] / rho_L;
+        }
     } else if (CRW[1] && ((u_star + c_star_R) < lu)) { /* sonic point in the 3-rarefaction, :315-339 */
         U[1] = zetaR * (u_R - 2.0 * (c_R - lu) / (gR - 1.0));
         C = lu - U[1];
@@ -416,6 +476,12 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
         D[0] = U[0] * (U[1] - lu) * pow(c_frac, (1.0 + zetaR) / zetaR) * TdS * (gR - 1.0);
         D[0] = (D[0] + D[3]) / C / C;
         D[2] = -(U[1] - lu) * d_v_R * U[0] / rho_R;
+        if (sc) {
+            UX[0] = XR->z;
+            UX[1] = XR->phi;
+            DX[0] = -(U[1] - lu) * XR->dz * U[0] / rho_R;
+            DX[1] = -(U[1] - lu) * XR->dphi * U[0] / rho_R;
+        }
     } else { /* non-sonic case, :340-523 */
         if (u_star < lu) {
             U[0] = rho_star_R; U[1] = u_star; U[2] = v_R; U[3] = p_star;
@@ -423,6 +489,11 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
         } else {
             U[0] = rho_star_L; U[1] = u_star; U[2] = v_L; U[3] = p_star;
             C = c_star_L;
+        }
+        if (sc) {
+            const orc_scal *Xu = (u_star < lu) ? XR : XL;
+            UX[0] = Xu->z;
+            UX[1] = Xu->phi;
         }
         if (CRW[0]) {
             a_L = 1.0;
@@ -481,6 +552,12 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
                 D[0] = (D[0] + D[3]) / c_star_R / c_star_R;
                 D[2] = -U[1] * d_v_R * U[0] / rho_R;
                 D[2] = D[2] + lu * d_v_R;
+                if (sc) {
+                    DX[0] = -U[1] * XR->dz * U[0] / rho_R;
+                    DX[0] = DX[0] + lu * XR->dz;
+                    DX[1] = -U[1] * XR->dphi * U[0] / rho_R;
+                    DX[1] = DX[1] + lu * XR->dphi;
+                }
             } else {
                 SmUs = sqrt(0.5 * ((gR + 1.0) * p_R + (gR - 1.0) * p_star) / rho_star_R);
                 SmUR = sqrt(0.5 * ((gR + 1.0) * p_star + (gR - 1.0) * p_R) / rho_R);
@@ -498,6 +575,12 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
                 D[0] = D[0] + lu * rho_x;
                 D[2] = -U[1] * SmUR * d_v_R / SmUs;
                 D[2] = D[2] + lu * d_v_R;
+                if (sc) {
+                    DX[0] = -U[1] * SmUR * XR->dz / SmUs;
+                    DX[0] = DX[0] + lu * XR->dz;
+                    DX[1] = -U[1] * SmUR * XR->dphi / SmUs;
+                    DX[1] = DX[1] + lu * XR->dphi;
+                }
             }
         } else {
             if (CRW[0]) {
@@ -505,6 +588,12 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
                 D[0] = (D[0] + D[3]) / c_star_L / c_star_L;
                 D[2] = -U[1] * d_v_L * U[0] / rho_L;
                 D[2] = D[2] + lu * d_v_L;
+                if (sc) {
+                    DX[0] = -U[1] * XL->dz * U[0] / rho_L;
+                    DX[0] = DX[0] + lu * XL->dz;
+                    DX[1] = -U[1] * XL->dphi * U[0] / rho_L;
+                    DX[1] = DX[1] + lu * XL->dphi;
+                }
             } else {
                 SmUs = -sqrt(0.5 * ((gL + 1.0) * p_L + (gL - 1.0) * p_star) / rho_star_L);
                 SmUL = -sqrt(0.5 * ((gL + 1.0) * p_star + (gL - 1.0) * p_L) / rho_L);
@@ -522,6 +611,12 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
                 D[0] = D[0] + lu * rho_x;
                 D[2] = -U[1] * SmUL * d_v_L / SmUs;
                 D[2] = D[2] + lu * d_v_L;
+                if (sc) {
+                    DX[0] = -U[1] * SmUL * XL->dz / SmUs;
+                    DX[0] = DX[0] + lu * XL->dz;
+                    DX[1] = -U[1] * SmUL * XL->dphi / SmUs;
+                    DX[1] = DX[1] + lu * XL->dphi;
+                }
             }
         }
     }
@@ -534,12 +629,20 @@ static void orc_q1d_solve(double gL, double gR, const orc_side *Ls, const orc_si
         D[1] = D[1] - (U[2] - lv) * T_u;
         D[2] = D[2] - (U[2] - lv) * t_v_L - T_p / U[0];
         D[3] = D[3] - (U[2] - lv) * T_p - U[0] * C * C * t_v_L;
+        if (sc) {
+            DX[0] = DX[0] - (U[2] - lv) * XL->tz;
+            DX[1] = DX[1] - (U[2] - lv) * XL->tphi;
+        }
     } else {
         T_rho = t_rho_R - t_p_R / (C * C) + T_p / (C * C);
         D[0] = D[0] - (U[2] - lv) * T_rho - U[0] * t_v_R;
         D[1] = D[1] - (U[2] - lv) * T_u;
         D[2] = D[2] - (U[2] - lv) * t_v_R - T_p / U[0];
         D[3] = D[3] - (U[2] - lv) * T_p - U[0] * C * C * t_v_R;
+        if (sc) {
+            DX[0] = DX[0] - (U[2] - lv) * XR->tz;
+            DX[1] = DX[1] - (U[2] - lv) * XR->tphi;
+        }
     }
 }
 
@@ -2564,6 +2667,102 @@ void orc_grp2d_flux(int cnt, const double *in, double tau, double eps, double *o
         for (int k = 0; k < 8; ++k)
             o[k] = o8[k];
         o[8] = rv;
+    }
+}
+
+/*
+ * GRP_2D_flux of the two-component build (flux_solver.c:158-237 with
+ * MULTIFLUID_BASICS): per-side gamma, passive volume fraction z and mass
+ * fraction phi through linear_GRP_solver_Edir_Q1D, the mixture gamma of the
+ * mid-time z (:203-208) in the energy flux, and the component fluxes and
+ * interface values of :221-235.
+ * in: cnt x 40 = n_x, n_y, then per side (left, right) gamma, rho,u,v,p,
+ *     d_rho,d_u,d_v,d_p, t_rho,t_u,t_v,t_p, z,d_z,t_z, phi,d_phi,t_phi.
+ * out: cnt x 19 = F_rho,F_u,F_v,F_e, RHO_int,U_int,V_int,P_int, F_phi,F_gamma,
+ *     F_e_a, PHI, Z_a, U_qt_add_c,V_qt_add_c, U_qt_star,V_qt_star, P_star,
+ *     return code.  gamma_a / gamma_b: config[6] / config[106]; store_gamma:
+ *     config[60] (F_gamma is written only when it is set, else 0).
+ */
+static void scal_from(orc_scal *x, const double *a)
+{
+    x->z = a[0]; x->dz = a[1]; x->tz = a[2];
+    x->phi = a[3]; x->dphi = a[4]; x->tphi = a[5];
+}
+
+void orc_grp2d_flux_mf(int cnt, const double *in, double tau, double eps, double gamma_a, double gamma_b,
+                       int store_gamma, double *out)
+{
+    for (int q = 0; q < cnt; ++q) {
+        const double *a = in + 40 * q;
+        const double n_x = a[0], n_y = a[1];
+        const double gL = a[2], gR = a[21];
+        orc_side L, R;
+        orc_scal XL, XR;
+        side_from(&L, a + 3);
+        scal_from(&XL, a + 15);
+        side_from(&R, a + 22);
+        scal_from(&XR, a + 34);
+        /* rotation into the face frame, :172-189 (z and phi are scalars) */
+        double u = L.u * n_x + L.v * n_y;
+        double u_R = R.u * n_x + R.v * n_y;
+        double d_u = L.du * n_x + L.dv * n_y;
+        double d_u_R = R.du * n_x + R.dv * n_y;
+        double t_u = L.tu * n_x + L.tv * n_y;
+        double t_u_R = R.tu * n_x + R.tv * n_y;
+        L.v = -L.u * n_y + L.v * n_x;
+        R.v = -R.u * n_y + R.v * n_x;
+        L.dv = -L.du * n_y + L.dv * n_x;
+        R.dv = -R.du * n_y + R.dv * n_x;
+        L.tv = -L.tu * n_y + L.tv * n_x;
+        R.tv = -R.tu * n_y + R.tv * n_x;
+        L.u = u;
+        R.u = u_R;
+        L.du = d_u;
+        R.du = d_u_R;
+        L.tu = t_u;
+        R.tu = t_u_R;
+
+        double ws[2], dire[4], mid[4], star[4], DX[2], UX[2];
+        orc_q1d_solve_x(gL, gR, &L, &R, &XL, &XR, eps, eps, ws, dire, mid, star, DX, UX, NULL, 0);
+        int rv = 0;
+        if (mid[3] < eps || mid[0] < eps)
+            rv = 1;
+        else if (!orc_isfinite4(mid))
+            rv = 2;
+        else if (!orc_isfinite4(dire))
+            rv = 3;
+
+        double rho_mid = mid[0] + 0.5 * tau * dire[0];
+        double u_mid = (mid[1] + 0.5 * tau * dire[1]) * n_x - (mid[2] + 0.5 * tau * dire[2]) * n_y;
+        double v_mid = (mid[1] + 0.5 * tau * dire[1]) * n_y + (mid[2] + 0.5 * tau * dire[2]) * n_x;
+        double p_mid = mid[3] + 0.5 * tau * dire[3];
+        double phi_mid = UX[1] + 0.5 * tau * DX[1];
+        double z_a_mid = UX[0] + 0.5 * tau * DX[0];
+        double gamma_mid = 1.0 / (z_a_mid / (gamma_a - 1.0) + (1.0 - z_a_mid) / (gamma_b - 1.0)) + 1.0;
+
+        double *o = out + 19 * q;
+        double F_rho = rho_mid * (u_mid * n_x + v_mid * n_y);
+        o[0] = F_rho;
+        o[1] = F_rho * u_mid + p_mid * n_x;
+        o[2] = F_rho * v_mid + p_mid * n_y;
+        double F_e = (gamma_mid / (gamma_mid - 1.0)) * p_mid / rho_mid + 0.5 * (u_mid * u_mid + v_mid * v_mid);
+        o[3] = F_rho * F_e;
+        o[5] = (mid[1] + tau * dire[1]) * n_x - (mid[2] + tau * dire[2]) * n_y;
+        o[6] = (mid[1] + tau * dire[1]) * n_y + (mid[2] + tau * dire[2]) * n_x;
+        o[4] = mid[0] + tau * dire[0];
+        o[7] = mid[3] + tau * dire[3];
+        o[8] = F_rho * phi_mid;
+        o[9] = store_gamma ? F_rho * gamma_mid : 0.0;
+        double F_e_a = z_a_mid / (gamma_a - 1.0) * p_mid / rho_mid + 0.5 * phi_mid * (u_mid * u_mid + v_mid * v_mid);
+        o[10] = F_rho * F_e_a;
+        o[11] = UX[1] + tau * DX[1];
+        o[12] = UX[0] + tau * DX[0];
+        o[13] = F_rho * u_mid * phi_mid;
+        o[14] = F_rho * v_mid * phi_mid;
+        o[15] = p_mid * n_x;
+        o[16] = p_mid * n_y;
+        o[17] = p_mid / rho_mid * F_rho;
+        o[18] = rv;
     }
 }
 

@@ -25,6 +25,9 @@ int orc_run_1d(int m, double *rho, double *u, double *p, double *E_out,
 void orc_riemann_exact(int cnt, const double *in, double eps, double tol, int N, double *out);
 void orc_riemann_exact_ben(int cnt, const double *in, double eps, double tol, int N, double *out);
 void orc_grp2d_flux(int cnt, const double *in, double tau, double eps, double *out);
+/* GRP_2D_flux of the two-component (MULTIFLUID_BASICS) build: rows of 40 in, 19 out. */
+void orc_grp2d_flux_mf(int cnt, const double *in, double tau, double eps, double gamma_a, double gamma_b,
+                       int store_gamma, double *out);
 void orc_q1d(int cnt, const double *in, double eps, double atc, double *out);
 void orc_g2d(int cnt, const double *in, double eps, double atc, double *out);
 int orc_run_1d_lag(int m, double *rho, double *u, double *p, double *E_out, double *X_out,

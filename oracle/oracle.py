@@ -26,6 +26,8 @@ CRPOW_SO = os.path.join(HERE, "_build", "libhydro_oracle_crpow.so")
 REF_SO = os.path.join(HERE, "_ref", "libhydro_ref.so")
 # the reference with GRP_2D_flux calling the genuinely-2D solver (oracle/Makefile)
 REF_G2D_SO = os.path.join(HERE, "_ref", "libhydro_ref_g2d.so")
+# GRP_2D_flux of the reference's two-component build (MULTIFLUID_BASICS)
+REF_MF_SO = os.path.join(HERE, "_ref", "libhydro_ref_mf.so")
 # Where oracle/Makefile finds the reference sources (only needed to build REF_SO).
 REF_TREE = os.environ.get("HYDRO_REFERENCE", "/root/reference")
 NCONF = 400
@@ -78,14 +80,21 @@ class Oracle:
         """which: "port" (the C restatement), "crpow" (the same with a correctly
         rounded pow), "reference" (the reference's own sources) or
         "reference_g2d" (the same with GRP_2D_flux calling the genuinely-2D
-        solver; the port selects it per run with config[301] = 1)."""
-        path = {"port": PORT_SO, "crpow": CRPOW_SO, "reference_g2d": REF_G2D_SO}.get(which, REF_SO)
+        solver; the port selects it per run with config[301] = 1) or
+        "reference_mf" (only the two-component interface flux, grp2d_flux_mf)."""
+        path = {"port": PORT_SO, "crpow": CRPOW_SO, "reference_g2d": REF_G2D_SO,
+                "reference_mf": REF_MF_SO}.get(which, REF_SO)
         if not os.path.exists(path):
             raise FileNotFoundError(f"oracle library missing: {path} (run make -C oracle)")
         self.which = which
         self.lib = ctypes.CDLL(path)
         p = "ref_" if which.startswith("reference") else "orc_"
         L = self.lib
+        self._fluxmf = getattr(L, p + "grp2d_flux_mf", None)
+        if self._fluxmf is not None:
+            self._fluxmf.argtypes = [_int, _dp, _dbl, _dbl, _dbl, _dbl, _int, _dp]
+        if which == "reference_mf":
+            return
         self._run2d = getattr(L, p + "run_2d")
         self._run2d.argtypes = [_int, _int, _dp, _dp, _dp, _dp, _dp, _dp, _int, _int, _int,
                                 ctypes.c_void_p, _int, ctypes.c_void_p, ctypes.POINTER(_int), _dp]
@@ -168,6 +177,17 @@ class Oracle:
         inp = np.ascontiguousarray(inp, np.float64)
         out = np.zeros((len(inp), 9))
         self._flux(len(inp), inp, tau, eps, out)
+        return out
+
+    def grp2d_flux_mf(self, inp, tau, eps=1e-9, gamma_a=1.4, gamma_b=1.4, store_gamma=True):
+        """Two-component GRP_2D_flux on rows of 40 (n_x, n_y, then per side gamma,
+        rho,u,v,p, d_rho,d_u,d_v,d_p, t_rho,t_u,t_v,t_p, z,d_z,t_z, phi,d_phi,t_phi);
+        returns rows of 19 (F_rho,F_u,F_v,F_e, RHO_int,U_int,V_int,P_int, F_phi,
+        F_gamma, F_e_a, PHI, Z_a, U_qt_add_c,V_qt_add_c, U_qt_star,V_qt_star,
+        P_star, return code).  gamma_a/gamma_b/store_gamma: config[6]/[106]/[60]."""
+        inp = np.ascontiguousarray(inp, np.float64)
+        out = np.zeros((len(inp), 19))
+        self._fluxmf(len(inp), inp, tau, eps, gamma_a, gamma_b, int(bool(store_gamma)), out)
         return out
 
     def q1d(self, inp, eps=1e-9, atc=1e-9):

@@ -51,6 +51,19 @@ def ref_g2d():
 
 
 @pytest.fixture(scope="session")
+def ref_mf():
+    """GRP_2D_flux of the reference's two-component build (MULTIFLUID_BASICS),
+    where the reference tree exists."""
+    import oracle as orc
+
+    if not os.path.exists(orc.REF_MF_SO):
+        if not orc.reference_available():
+            pytest.skip("reference tree not present on this machine")
+        orc.build(ref=True)
+    return orc.Oracle("reference_mf")
+
+
+@pytest.fixture(scope="session")
 def gpu_lib():
     import torch
 

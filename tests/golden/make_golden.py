@@ -9,10 +9,13 @@ reference tree; the fixtures travel with the repository.
     python tests/golden/make_golden.py --large    # also the 1024^2 x 500 run summary
     python tests/golden/make_golden.py --only g2d # only the genuinely-2D solver's fixtures
     python tests/golden/make_golden.py --only lag # only the 1D Lagrangian schemes' fixtures
+    python tests/golden/make_golden.py --only mf  # only the two-component interface flux
 
 The genuinely-2D GRP fixtures come from oracle/_ref/libhydro_ref_g2d.so, the
 same sources with GRP_2D_flux calling linear_GRP_solver_Edir_G2D (the
-alternative the reference keeps commented out at flux_solver.c:189).
+alternative the reference keeps commented out at flux_solver.c:189).  The
+two-component interface-flux fixture comes from oracle/_ref/libhydro_ref_mf.so
+(GRP_2D_flux compiled with MULTIFLUID_BASICS).
 """
 from __future__ import annotations
 
@@ -177,6 +180,41 @@ def lag_runs():
     return runs
 
 
+def mf_inputs(rng, n):
+    """Two-component interface pairs (rows of 40, the layout of the oracle's
+    grp2d_flux_mf): the wave mix of g2d_inputs with a gamma per side, volume
+    and mass fractions with random slopes, axis and oblique normals."""
+    q = g2d_inputs(rng, n)
+    L, R = q[:, 1:13], q[:, 13:25]
+
+    def scal(k):
+        return np.column_stack([rng.uniform(0, 1, k), rng.normal(0, 1, k), rng.normal(0, 1, k),
+                                rng.uniform(0, 1, k), rng.normal(0, 1, k), rng.normal(0, 1, k)])
+    gL = rng.uniform(1.1, 3.0, n)
+    gR = rng.uniform(1.1, 3.0, n)
+    k = n // 8
+    gR[4 * k:5 * k] = gL[4 * k:5 * k]                                # one gamma on both sides
+    th = rng.uniform(0, 2 * np.pi, n)
+    normals = np.column_stack([np.cos(th), np.sin(th)])
+    normals[: n // 4] = [1.0, 0.0]
+    normals[n // 4: n // 2] = [0.0, 1.0]
+    return np.column_stack([normals, gL, L, scal(n), gR, R, scal(n)])
+
+
+MF_GAMMA_A, MF_GAMMA_B = 1.4, 3.0   # config[6], config[106]
+
+
+def make_mf():
+    R = orc.Oracle("reference_mf")
+    rng = np.random.default_rng(20261205)
+    inp = mf_inputs(rng, 1024)
+    tau = 1e-3
+    np.savez_compressed(os.path.join(HERE, "grp2d_flux_mf.npz"), inp=inp, tau=tau,
+                        gamma_a=MF_GAMMA_A, gamma_b=MF_GAMMA_B,
+                        out=R.grp2d_flux_mf(inp, tau, 1e-9, MF_GAMMA_A, MF_GAMMA_B, True),
+                        out_nogamma=R.grp2d_flux_mf(inp, tau, 1e-9, MF_GAMMA_A, MF_GAMMA_B, False))
+
+
 def make_lag():
     R = orc.Oracle("reference")
     rng = np.random.default_rng(20261204)
@@ -197,13 +235,15 @@ def make_lag():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
-    ap.add_argument("--only", choices=["all", "g2d", "lag"], default="all")
+    ap.add_argument("--only", choices=["all", "g2d", "lag", "mf"], default="all")
     args = ap.parse_args()
     orc.build(ref=True)
     if args.only in ("all", "g2d"):
         make_g2d()
     if args.only in ("all", "lag"):
         make_lag()
+    if args.only in ("all", "mf"):
+        make_mf()
     if args.only != "all":
         print("fixtures written to", HERE)
         return

@@ -235,3 +235,63 @@ def test_lag_port_matches_reference_random(port, ref):
         a, b = port.run_1d_lag(rho, u, p, cfg, order), ref.run_1d_lag(rho, u, p, cfg, order)
         for f in ("rho", "u", "p", "E", "X"):
             assert np.array_equal(a[f], b[f])
+
+
+# -- two-component (MULTIFLUID_BASICS) interface flux --------------------------
+
+def _mf_rows_equal(got, want):
+    """Same return code everywhere; outputs bit for bit where the reference
+    returned 0 (on a failed check it returns before writing them)."""
+    assert np.array_equal(got[:, 18], want[:, 18])
+    ok = want[:, 18] == 0
+    assert np.array_equal(got[ok], want[ok])
+
+
+def test_mf_flux_golden(port):
+    """The two-component GRP_2D_flux against the reference's MULTIFLUID build:
+    per-side gamma, volume/mass fractions, mixture gamma, F_gamma on and off."""
+    d = load("grp2d_flux_mf.npz")
+    tau, ga, gb = float(d["tau"]), float(d["gamma_a"]), float(d["gamma_b"])
+    _mf_rows_equal(port.grp2d_flux_mf(d["inp"], tau, 1e-9, ga, gb, True), d["out"])
+    _mf_rows_equal(port.grp2d_flux_mf(d["inp"], tau, 1e-9, ga, gb, False), d["out_nogamma"])
+    out = d["out"]
+    assert (out[:, 18] == 0).mean() > 0.9
+    assert np.all(d["out_nogamma"][out[:, 18] == 0, 9] == 0.0)
+
+
+def test_mf_flux_reduces_to_single_fluid(port):
+    """One gamma on both sides equal to config[6] and z = 1 with flat z: the
+    mixture gamma is config[6] and the gas-dynamic outputs are those of the
+    single-fluid GRP_2D_flux, bit for bit; the component fluxes follow from
+    them (F_phi = F_rho phi_mid with phi_mid = PHI at tau/2)."""
+    d = load("grp2d_flux_mf.npz")
+    inp = d["inp"].copy()
+    g = 1.4
+    inp[:, 2] = g
+    inp[:, 21] = g
+    inp[:, 15] = inp[:, 34] = 1.0
+    inp[:, [16, 17, 35, 36]] = 0.0
+    mf = port.grp2d_flux_mf(inp, 1e-3, 1e-9, g, 3.0, True)
+    single = np.column_stack([inp[:, 0], inp[:, 1], np.full(len(inp), g), inp[:, 3:15], inp[:, 22:34]])
+    sf = port.grp2d_flux(single, 1e-3)
+    ok = sf[:, 8] == 0
+    assert np.array_equal(mf[:, 18], sf[:, 8])
+    assert np.array_equal(mf[ok, :8], sf[ok, :8])
+    assert np.array_equal(mf[ok, 12], np.ones(ok.sum()))           # Z_a stays 1
+    np.testing.assert_allclose(mf[ok, 9], mf[ok, 0] * g, rtol=1e-15)  # F_gamma = F_rho gamma_mid
+
+
+def test_mf_port_matches_reference_random(port, ref_mf):
+    """Fresh random two-component faces (wide state ranges, any normal)
+    against the reference's MULTIFLUID build."""
+    rng = np.random.default_rng(321)
+    n = 3000
+
+    def side():
+        return np.column_stack([rng.uniform(1.05, 4.0, n), np.exp(rng.uniform(-3, 3, n)), rng.uniform(-3, 3, (n, 2)),
+                                np.exp(rng.uniform(-3, 3, n)), rng.normal(0, 2, (n, 8)), rng.uniform(0, 1, n),
+                                rng.normal(0, 1, (n, 2)), rng.uniform(0, 1, n), rng.normal(0, 1, (n, 2))])
+    th = rng.uniform(0, 2 * np.pi, n)
+    inp = np.column_stack([np.cos(th), np.sin(th), side(), side()])
+    for ga, gb, sg in ((1.4, 3.0, True), (1.67, 1.2, False)):
+        _mf_rows_equal(port.grp2d_flux_mf(inp, 2e-3, 1e-9, ga, gb, sg), ref_mf.grp2d_flux_mf(inp, 2e-3, 1e-9, ga, gb, sg))
