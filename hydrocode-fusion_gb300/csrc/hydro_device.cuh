@@ -296,6 +296,103 @@ __device__ __forceinline__ R slope_right(R pp, R pR, R cR, const Gas<R>& G)
     return t1 * t2;
 }
 
+// Powers of one base x with the logarithm computed once: pow(y) equals
+// M<R>::pow_(x, y) bit for bit (for FP64 it is dd_pow's own path after its
+// logarithm).  The wave curve of a rarefaction side and the curve's slope need
+// x^mu and x^nu of the same pressure ratio.
+template <typename R> struct PowBase;
+template <> struct PowBase<double> {
+    double x, lh, ll;
+    bool dd;  // x in (0, inf): the double-double path of dd_pow
+    __device__ __forceinline__ void init(double x_)
+    {
+        x = x_;
+        dd = (x > 0.0) && (x < INFINITY);
+        lh = ll = 0.0;
+        if (dd)
+            dd_log(x, lh, ll);
+    }
+    __device__ __forceinline__ double pow(double y) const
+    {
+        if (!dd || !(y - y == 0.0))
+            return ::pow(x, y);
+        if (y == 0.0 || x == 1.0)
+            return 1.0;
+        const double th = y * lh;
+        const double tl = fma(y, lh, -th) + y * ll;
+        if (!(fabs(th) < 700.0))
+            return ::pow(x, y);
+        return dd_exp(th, tl);
+    }
+};
+template <> struct PowBase<float> {
+    float l2;
+    __device__ __forceinline__ void init(float x) { l2 = __log2f(x); }
+    __device__ __forceinline__ float pow(float y) const { return exp2f(y * l2); }
+};
+
+// One side's wave curve at pressure pp (curve_left / curve_right) and the
+// curve's slope there (slope_left / slope_right, k1 / k3 of the Newton loop),
+// computed together so that they share the square root of a shock side and the
+// logarithm of a rarefaction side; each value equals the separate function's
+// bit for bit.  LEFT: the 1-wave (u - w), else the 3-wave (u + w).
+template <typename R>
+struct CurveSlope {
+    R v, k;
+};
+
+template <typename R, bool LEFT>
+__device__ __forceinline__ CurveSlope<R> curve_slope_body(R pp, R u, R p, R c, const Gas<R>& G)
+{
+    CurveSlope<R> r;
+    R w;
+    const R t2 = c / G.g / p;
+    if (pp > p) {
+        const R dp = pp - p;
+        const R sq = M<R>::sqrt_(R(1) + G.nu * dp / p);
+        w = dp * c / G.g / p / sq;
+        const R t1 = R(1) / sq;
+        const R t3 = R(0.5) * t2 * G.nu / p;
+        const R cube = M<R>::pow_(t1, R(3));
+        r.k = LEFT ? t3 * dp * cube - t2 * t1 : t2 * t1 - t3 * dp * cube;
+    } else {
+        PowBase<R> pb;
+        pb.init(pp / p);
+        w = pb.pow(G.mu) - R(1);
+        w = R(2) * c * w / G.gm1;
+        const R t1 = R(1) / pb.pow(G.nu);
+        r.k = LEFT ? -t1 * t2 : t1 * t2;
+    }
+    r.v = LEFT ? u - w : u + w;
+    return r;
+}
+
+// FP64: out of line (its double-double temporaries stay out of the callers'
+// register allocation; the result comes back in registers).
+template <bool LEFT>
+__device__ __noinline__ CurveSlope<double> curve_slope_f64(double pp, double u, double p, double c, double g,
+                                                          double gm1, double mu, double nu)
+{
+    Gas<double> G;
+    G.g = g;
+    G.gm1 = gm1;
+    G.mu = mu;
+    G.nu = nu;
+    return curve_slope_body<double, LEFT>(pp, u, p, c, G);
+}
+
+template <typename R, bool LEFT>
+__device__ __forceinline__ void curve_slope_at(R pp, R u, R p, R c, const Gas<R>& G, R& v, R& k)
+{
+    CurveSlope<R> r;
+    if constexpr (sizeof(R) == 8)
+        r = curve_slope_f64<LEFT>(pp, u, p, c, G.g, G.gm1, G.mu, G.nu);
+    else
+        r = curve_slope_body<R, LEFT>(pp, u, p, c, G);
+    v = r.v;
+    k = r.k;
+}
+
 struct StarInfo {
     int iters;     // Newton iterations taken (-1 when the uniform-pair shortcut was used)
     int crw0, crw1;
@@ -320,28 +417,30 @@ __device__ __forceinline__ void exact_riemann(R uL, R uR, R pL, R pR, R cL, R cR
         p_int = (pL < pR) ? pL : pR;
     p_int = R(0.5) * p_int;
 
-    R vL = curve_left(p_int, uL, pL, cL, G);
-    R vR = curve_right(p_int, uR, pR, cR, G);
-    R gap = M<R>::abs_(vL - vR);
-
     if (M<R>::abs_(uL - uR) < tol && M<R>::abs_(pL - pR) < tol) {
         p_star = R(0.5) * (pL + pR);
         u_star = R(0.5) * (uL + uR);
         st.iters = 0;
         return;
     }
+    // curves and slopes at the current pressure (the slopes are the next
+    // iteration's k1, k3; k1, k3 themselves stay those of the last iteration)
+    R vL, vR, k1n, k3n;
+    curve_slope_at<R, true>(p_int, uL, pL, cL, G, vL, k1n);
+    curve_slope_at<R, false>(p_int, uR, pR, cR, G, vR, k3n);
+    R gap = M<R>::abs_(vL - vR);
     int it = 0;
     while ((gap > tol) && (it != N)) {
-        k1 = slope_left(p_int, pL, cL, G);
-        k3 = slope_right(p_int, pR, cR, G);
+        k1 = k1n;
+        k3 = k3n;
         R p_new = p_int + (vR - vL) / (k1 - k3);
         if (p_new < R(0))
             p_int = R(0.5) * p_int;
         else
             p_int = p_new;
         ++it;
-        vL = curve_left(p_int, uL, pL, cL, G);
-        vR = curve_right(p_int, uR, pR, cR, G);
+        curve_slope_at<R, true>(p_int, uL, pL, cL, G, vL, k1n);
+        curve_slope_at<R, false>(p_int, uR, pR, cR, G, vR, k3n);
         gap = M<R>::abs_(vL - vR);
     }
     u_star = k1 * (vR - vL) / (k1 - k3) + vL;

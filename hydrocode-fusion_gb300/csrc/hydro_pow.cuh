@@ -132,12 +132,29 @@ HYDRO_HD static inline double dd_exp(double th, double tl)
     return r * bits_to_double((uint64_t)(q + 1023) << 52);
 }
 
+// x^3 for 2^-300 < x < 2^300: x*x exactly as a double-double (fma), times x
+// again with the product's high part exact, so the value before the final
+// rounding is within about 2^-104 of x^3 -- a correctly rounded cube except for
+// arguments within that distance of a rounding boundary, which is far tighter
+// than the general path's ~2^-70.  (The solvers' Newton slope takes
+// pow(t, 3.0) of every shock side in every iteration.)
+HYDRO_HD static inline double dd_cube(double x)
+{
+    const double ph = x * x;
+    const double pl = fma(x, x, -ph);
+    const double qh = ph * x;
+    const double ql = fma(ph, x, -qh) + pl * x;
+    return qh + ql;
+}
+
 HYDRO_HD static inline double dd_pow(double x, double y)
 {
     if (!(x > 0.0) || !(x < INFINITY) || !(y - y == 0.0))
         return pow(x, y);
     if (y == 0.0 || x == 1.0)
         return 1.0;
+    if (y == 3.0 && x > 0x1p-300 && x < 0x1p300)
+        return dd_cube(x);
     double lh, ll;
     dd_log(x, lh, ll);
     const double th = y * lh;

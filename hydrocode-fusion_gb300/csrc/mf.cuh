@@ -69,15 +69,15 @@ __device__ __noinline__ bool mf_exact(double uL, double uR, double pL, double pR
         p_int = NW.p;
         it = NW.it;
     }
-    double vL = curve_left(p_int, uL, pL, cL, GL);
-    double vR = curve_right(p_int, uR, pR, cR, GR);
-    double gap = fabs(vL - vR);
-
     if (fabs(uL - uR) < eps && fabs(pL - pR) < eps) {
         p_star = 0.5 * (pL + pR);
         u_star = 0.5 * (uL + uR);
         return false;
     }
+    double vL, vR, k1n, k3n;   // curves and slopes at p_int (the slopes: the next iteration's k1, k3)
+    curve_slope_at<double, true>(p_int, uL, pL, cL, GL, vL, k1n);
+    curve_slope_at<double, false>(p_int, uR, pR, cR, GR, vR, k3n);
+    double gap = fabs(vL - vR);
     const int stop = it + cap;
     while ((gap > eps) && (it != 500)) {
         if (it >= stop) {
@@ -85,13 +85,13 @@ __device__ __noinline__ bool mf_exact(double uL, double uR, double pL, double pR
             NW.it = it;
             return true;
         }
-        k1 = slope_left(p_int, pL, cL, GL);
-        k3 = slope_right(p_int, pR, cR, GR);
+        k1 = k1n;
+        k3 = k3n;
         const double p_new = p_int + (vR - vL) / (k1 - k3);
         p_int = (p_new < 0.0) ? 0.5 * p_int : p_new;
         ++it;
-        vL = curve_left(p_int, uL, pL, cL, GL);
-        vR = curve_right(p_int, uR, pR, cR, GR);
+        curve_slope_at<double, true>(p_int, uL, pL, cL, GL, vL, k1n);
+        curve_slope_at<double, false>(p_int, uR, pR, cR, GR, vR, k3n);
         gap = fabs(vL - vR);
     }
     u_star = k1 * (vR - vL) / (k1 - k3) + vL;

@@ -55,3 +55,24 @@ def test_dd_pow_matches_libm():
     x[: n // 4] = 1.0 + rng.normal(0, 1e-6, n // 4)  # ratios near 1 (Newton near convergence)
     _check(L, x, y)
     _check(L, np.exp(rng.uniform(-5, 5, n)), rng.uniform(-8, 8, n))
+
+
+def test_dd_cube_is_correctly_rounded():
+    """pow(t, 3.0) takes the double-double cube: on random arguments across the
+    range it returns the correctly rounded cube (exact in 60-digit decimal
+    arithmetic), and it agrees with the C library wherever that one is
+    correctly rounded."""
+    L = _lib()
+    rng = np.random.default_rng(3)
+    n = 200_000
+    x = np.concatenate([rng.uniform(0, 1, n // 2), np.exp(rng.uniform(-300, 300, n // 2) * np.log(2.0) / 1.2)])
+    y = np.full(n, 3.0)
+    a, b = np.zeros(n), np.zeros(n)
+    L.pow_pair(x, y, n, a, b)
+    getcontext().prec = 60
+    for i in rng.choice(n, 3000, replace=False):
+        assert a[i] == float(Decimal(float(x[i])) ** 3), x[i]
+    for i in np.nonzero(a != b)[0][:200]:
+        t = Decimal(float(x[i])) ** 3
+        assert abs(Decimal(float(a[i])) - t) <= abs(Decimal(float(b[i])) - t), x[i]
+    assert (a != b).mean() < 1e-3
