@@ -396,7 +396,7 @@ def mf_suite(hg, peak, nface=8 << 20, reps=5, cpu=True):
                    "h2d_bytes": 40 * 8 * nface, "d2h_bytes": (18 * 8 + 4) * nface},
            "hbm": {"bytes_per_face": MF_BYTES_PER_FACE,
                    "achieved_gbs": MF_BYTES_PER_FACE * nface / (k_ms * 1e-3) / 1e9, "peak_gbs": peak},
-           "bad_faces": int(info.n_bad), "resumed_faces": [int(info.resumed[0]), int(info.resumed[1])]}
+           "bad_faces": int(info.n_bad), "resumed_faces": [int(r) for r in info.resumed]}
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as orc

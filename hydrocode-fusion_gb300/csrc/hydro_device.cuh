@@ -341,27 +341,42 @@ struct CurveSlope {
     R v, k;
 };
 
+// The per-side quantities of the slope that do not change with the pressure:
+// t2 = c / gamma / p and t3 = 0.5 t2 nu / p (slope_left :136-149, slope_right
+// :150-164 recompute them every iteration; the values are the same).
+template <typename R>
+struct SideConst {
+    R t2, t3;
+};
+
+template <typename R>
+__device__ __forceinline__ SideConst<R> side_const(R p, R c, const Gas<R>& G)
+{
+    SideConst<R> s;
+    s.t2 = c / G.g / p;
+    s.t3 = R(0.5) * s.t2 * G.nu / p;
+    return s;
+}
+
 template <typename R, bool LEFT>
-__device__ __forceinline__ CurveSlope<R> curve_slope_body(R pp, R u, R p, R c, const Gas<R>& G)
+__device__ __forceinline__ CurveSlope<R> curve_slope_body(R pp, R u, R p, R c, const Gas<R>& G, SideConst<R> K)
 {
     CurveSlope<R> r;
     R w;
-    const R t2 = c / G.g / p;
     if (pp > p) {
         const R dp = pp - p;
         const R sq = M<R>::sqrt_(R(1) + G.nu * dp / p);
         w = dp * c / G.g / p / sq;
         const R t1 = R(1) / sq;
-        const R t3 = R(0.5) * t2 * G.nu / p;
         const R cube = M<R>::pow_(t1, R(3));
-        r.k = LEFT ? t3 * dp * cube - t2 * t1 : t2 * t1 - t3 * dp * cube;
+        r.k = LEFT ? K.t3 * dp * cube - K.t2 * t1 : K.t2 * t1 - K.t3 * dp * cube;
     } else {
         PowBase<R> pb;
         pb.init(pp / p);
         w = pb.pow(G.mu) - R(1);
         w = R(2) * c * w / G.gm1;
         const R t1 = R(1) / pb.pow(G.nu);
-        r.k = LEFT ? -t1 * t2 : t1 * t2;
+        r.k = LEFT ? -t1 * K.t2 : t1 * K.t2;
     }
     r.v = LEFT ? u - w : u + w;
     return r;
@@ -371,24 +386,24 @@ __device__ __forceinline__ CurveSlope<R> curve_slope_body(R pp, R u, R p, R c, c
 // register allocation; the result comes back in registers).
 template <bool LEFT>
 __device__ __noinline__ CurveSlope<double> curve_slope_f64(double pp, double u, double p, double c, double g,
-                                                          double gm1, double mu, double nu)
+                                                          double gm1, double mu, double nu, double t2, double t3)
 {
     Gas<double> G;
     G.g = g;
     G.gm1 = gm1;
     G.mu = mu;
     G.nu = nu;
-    return curve_slope_body<double, LEFT>(pp, u, p, c, G);
+    return curve_slope_body<double, LEFT>(pp, u, p, c, G, SideConst<double>{t2, t3});
 }
 
 template <typename R, bool LEFT>
-__device__ __forceinline__ void curve_slope_at(R pp, R u, R p, R c, const Gas<R>& G, R& v, R& k)
+__device__ __forceinline__ void curve_slope_at(R pp, R u, R p, R c, const Gas<R>& G, SideConst<R> K, R& v, R& k)
 {
     CurveSlope<R> r;
     if constexpr (sizeof(R) == 8)
-        r = curve_slope_f64<LEFT>(pp, u, p, c, G.g, G.gm1, G.mu, G.nu);
+        r = curve_slope_f64<LEFT>(pp, u, p, c, G.g, G.gm1, G.mu, G.nu, K.t2, K.t3);
     else
-        r = curve_slope_body<R, LEFT>(pp, u, p, c, G);
+        r = curve_slope_body<R, LEFT>(pp, u, p, c, G, K);
     v = r.v;
     k = r.k;
 }
@@ -401,7 +416,11 @@ struct StarInfo {
 
 // Exact Riemann solver, riemann_solver_exact_Ben.c:30-211 (single gamma).
 // Starting pressure: the reference's half linearised intersection (:86-93).
-template <typename R>
+// FUSED: each Newton pressure's curves and slopes come from curve_slope_at;
+// otherwise the curves and slopes are evaluated separately, as the reference
+// writes them (the same values; the FP32 forms' FP64 retry keeps this form,
+// whose smaller footprint leaves their kernels' register allocation alone).
+template <typename R, bool FUSED = true>
 __device__ __forceinline__ void exact_riemann(R uL, R uR, R pL, R pR, R cL, R cR, R tol, int N,
                                               const Gas<R>& G, R& u_star, R& p_star, StarInfo& st)
 {
@@ -423,11 +442,35 @@ __device__ __forceinline__ void exact_riemann(R uL, R uR, R pL, R pR, R cL, R cR
         st.iters = 0;
         return;
     }
+    if constexpr (!FUSED) {
+        R vL = curve_left(p_int, uL, pL, cL, G);
+        R vR = curve_right(p_int, uR, pR, cR, G);
+        R gap = M<R>::abs_(vL - vR);
+        int it = 0;
+        while ((gap > tol) && (it != N)) {
+            k1 = slope_left(p_int, pL, cL, G);
+            k3 = slope_right(p_int, pR, cR, G);
+            R p_new = p_int + (vR - vL) / (k1 - k3);
+            if (p_new < R(0))
+                p_int = R(0.5) * p_int;
+            else
+                p_int = p_new;
+            ++it;
+            vL = curve_left(p_int, uL, pL, cL, G);
+            vR = curve_right(p_int, uR, pR, cR, G);
+            gap = M<R>::abs_(vL - vR);
+        }
+        u_star = k1 * (vR - vL) / (k1 - k3) + vL;
+        p_star = p_int;
+        st.iters = it;
+        return;
+    }
     // curves and slopes at the current pressure (the slopes are the next
     // iteration's k1, k3; k1, k3 themselves stay those of the last iteration)
     R vL, vR, k1n, k3n;
-    curve_slope_at<R, true>(p_int, uL, pL, cL, G, vL, k1n);
-    curve_slope_at<R, false>(p_int, uR, pR, cR, G, vR, k3n);
+    const SideConst<R> KL = side_const(pL, cL, G), KR = side_const(pR, cR, G);
+    curve_slope_at<R, true>(p_int, uL, pL, cL, G, KL, vL, k1n);
+    curve_slope_at<R, false>(p_int, uR, pR, cR, G, KR, vR, k3n);
     R gap = M<R>::abs_(vL - vR);
     int it = 0;
     while ((gap > tol) && (it != N)) {
@@ -439,8 +482,8 @@ __device__ __forceinline__ void exact_riemann(R uL, R uR, R pL, R pR, R cL, R cR
         else
             p_int = p_new;
         ++it;
-        curve_slope_at<R, true>(p_int, uL, pL, cL, G, vL, k1n);
-        curve_slope_at<R, false>(p_int, uR, pR, cR, G, vR, k3n);
+        curve_slope_at<R, true>(p_int, uL, pL, cL, G, KL, vL, k1n);
+        curve_slope_at<R, false>(p_int, uR, pR, cR, G, KR, vR, k3n);
         gap = M<R>::abs_(vL - vR);
     }
     u_star = k1 * (vR - vL) / (k1 - k3) + vL;
@@ -477,11 +520,12 @@ template <typename R> struct StarPolicy;
 
 template <> struct StarPolicy<double> {
     static __device__ __forceinline__ bool uniform(double dist, double, const Gas<double>& G) { return dist < G.eps; }
+    template <bool FUSED = true>
     static __device__ __forceinline__ void solve(double uL, double uR, double pL, double pR, double cL, double cR,
                                                  const Gas<double>& G, double, double& u_star, double& p_star,
                                                  StarInfo& st)
     {
-        exact_riemann(uL, uR, pL, pR, cL, cR, G.eps, 500, G, u_star, p_star, st);
+        exact_riemann<double, FUSED>(uL, uR, pL, pR, cL, cR, G.eps, 500, G, u_star, p_star, st);
         st.fallback = 0;
     }
 };
@@ -498,6 +542,7 @@ template <> struct StarPolicy<float> {
     {
         return dist < fmaxf(G.eps, 1e-6f * scale);
     }
+    template <bool FUSED = true>  // (FP32: one form)
     static __device__ void solve(float uL, float uR, float pL, float pR, float cL, float cR, const Gas<float>& G,
                                  float p_start, float& u_star, float& p_star, StarInfo& st)
     {
@@ -558,7 +603,7 @@ static __device__ __noinline__ void exact_riemann_fp64_fallback(float uL, float 
     D.nu = (g + 1.0) / (2.0 * g);
     D.eps = eps;
     double us, ps;
-    exact_riemann<double>((double)uL, (double)uR, (double)pL, (double)pR, (double)cL, (double)cR, eps, 500, D, us, ps,
+    exact_riemann<double, false>((double)uL, (double)uR, (double)pL, (double)pR, (double)cL, (double)cR, eps, 500, D, us, ps,
                           st);
     u_star = (float)us;
     p_star = (float)ps;
@@ -570,11 +615,11 @@ __device__ __forceinline__ void q1d_waves(const Side<R>& L, const Side<R>& Rr, c
 // Non-uniform pairs: exact solver and the waves of the star state.  Out of line:
 // only a few percent of the faces of piecewise-smooth data get here, and
 // keeping it separate leaves the common (uniform-pair) path its registers.
-template <typename R>
+template <typename R, bool FUSED = true>
 __device__ __noinline__ void q1d_star_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
                                             StarInfo& st, R p_start)
 {
-    StarPolicy<R>::solve(L.u, Rr.u, L.p, Rr.p, S.c_L, S.c_R, G, p_start, S.u_star, S.p_star, st);
+    StarPolicy<R>::template solve<FUSED>(L.u, Rr.u, L.p, Rr.p, S.c_L, S.c_R, G, p_start, S.u_star, S.p_star, st);
     S.crw0 = st.crw0;
     S.crw1 = st.crw1;
     q1d_waves(L, Rr, G, S);
@@ -605,8 +650,8 @@ __device__ __forceinline__ bool face_uniform(const Side<R>& L, const Side<R>& Rr
 
 // KNOWN: 0 = make the uniform-pair decision here; 1 / 2 = the caller has
 // already made it with face_uniform (1 uniform, 2 not), so only that branch
-// is compiled into the caller.
-template <typename R, int KNOWN = 0, int RS = 0>
+// is compiled into the caller.  FUSED: as for exact_riemann.
+template <typename R, int KNOWN = 0, int RS = 0, bool FUSED = true>
 __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
                                          StarInfo& st, R p_start = R(-1))
 {
@@ -633,7 +678,7 @@ __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, co
         return;
     }
     if constexpr (KNOWN != 1)  // no out-of-line call (and its addressed arguments) on the uniform path
-        q1d_star_exact(L, Rr, G, S, st, p_start);
+        q1d_star_exact<R, FUSED>(L, Rr, G, S, st, p_start);
 }
 
 // Waves of the star state (linear_grp_solver_Edir_Q1D.c:110-133).

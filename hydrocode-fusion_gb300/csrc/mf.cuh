@@ -40,49 +40,66 @@ struct MfScal {
 struct MfNewton {
     double p;
     int it;
+    int crw;  // wave pattern, once known: 4 | crw0 << 1 | crw1 (0: not yet computed)
 };
 
 // Exact two-gamma Riemann solver: GL on the 1-wave side, GR on the 3-wave side
 // (riemann_solver_exact_Ben.c:30-211).  tol and eps are both config[4].
 // At most `cap` iterations are taken in this call (cap >= 500: the reference's
 // limit alone); when the cap stops an unfinished iteration, NW holds its state
-// and the function returns true.  resume: continue from NW instead of the
-// reference's starting pressure.
+// and the function returns true.  cap == 0 only classifies: the wave pattern and
+// the starting pressure go to NW (true is returned unless the trivial case
+// settles the face).  resume: continue from NW instead of the reference's
+// starting pressure.
 __device__ __noinline__ bool mf_exact(double uL, double uR, double pL, double pR, double cL, double cR, double eps,
                                       const Gas<double>& GL, const Gas<double>& GR, double& u_star, double& p_star,
                                       int& crw0, int& crw1, int cap, bool resume, MfNewton& NW)
 {
-    const double uLR = curve_left(pR, uL, pL, cL, GL);
-    const double uRL = curve_right(pL, uR, pR, cR, GR);
-    crw1 = (uLR > uR + eps) ? 0 : 1;
-    crw0 = (uRL > uL - eps) ? 1 : 0;
+    if (resume && NW.crw) {
+        crw0 = (NW.crw >> 1) & 1;
+        crw1 = NW.crw & 1;
+    } else {
+        const double uLR = curve_left(pR, uL, pL, cL, GL);
+        const double uRL = curve_right(pL, uR, pR, cR, GR);
+        crw1 = (uLR > uR + eps) ? 0 : 1;
+        crw0 = (uRL > uL - eps) ? 1 : 0;
+    }
 
     double k1 = -cL / pL / GL.g;
     double k3 = cR / pR / GR.g;
-    double p_int = (k1 * pL - k3 * pR - uL + uR) / (k1 - k3);
-    if (p_int < 0.0)
-        p_int = (pL < pR) ? pL : pR;
-    p_int = 0.5 * p_int;
-
+    double p_int;
     int it = 0;
     if (resume) {
         p_int = NW.p;
         it = NW.it;
+    } else {
+        p_int = (k1 * pL - k3 * pR - uL + uR) / (k1 - k3);
+        if (p_int < 0.0)
+            p_int = (pL < pR) ? pL : pR;
+        p_int = 0.5 * p_int;
     }
     if (fabs(uL - uR) < eps && fabs(pL - pR) < eps) {
         p_star = 0.5 * (pL + pR);
         u_star = 0.5 * (uL + uR);
         return false;
     }
+    if (cap == 0) {
+        NW.p = p_int;
+        NW.it = 0;
+        NW.crw = 4 | crw0 << 1 | crw1;
+        return true;
+    }
     double vL, vR, k1n, k3n;   // curves and slopes at p_int (the slopes: the next iteration's k1, k3)
-    curve_slope_at<double, true>(p_int, uL, pL, cL, GL, vL, k1n);
-    curve_slope_at<double, false>(p_int, uR, pR, cR, GR, vR, k3n);
+    const SideConst<double> KL = side_const(pL, cL, GL), KR = side_const(pR, cR, GR);
+    curve_slope_at<double, true>(p_int, uL, pL, cL, GL, KL, vL, k1n);
+    curve_slope_at<double, false>(p_int, uR, pR, cR, GR, KR, vR, k3n);
     double gap = fabs(vL - vR);
     const int stop = it + cap;
     while ((gap > eps) && (it != 500)) {
         if (it >= stop) {
             NW.p = p_int;
             NW.it = it;
+            NW.crw = 4 | crw0 << 1 | crw1;
             return true;
         }
         k1 = k1n;
@@ -90,8 +107,8 @@ __device__ __noinline__ bool mf_exact(double uL, double uR, double pL, double pR
         const double p_new = p_int + (vR - vL) / (k1 - k3);
         p_int = (p_new < 0.0) ? 0.5 * p_int : p_new;
         ++it;
-        curve_slope_at<double, true>(p_int, uL, pL, cL, GL, vL, k1n);
-        curve_slope_at<double, false>(p_int, uR, pR, cR, GR, vR, k3n);
+        curve_slope_at<double, true>(p_int, uL, pL, cL, GL, KL, vL, k1n);
+        curve_slope_at<double, false>(p_int, uR, pR, cR, GR, KR, vR, k3n);
         gap = fabs(vL - vR);
     }
     u_star = k1 * (vR - vL) / (k1 - k3) + vL;

@@ -45,20 +45,31 @@ __device__ __forceinline__ void mf_load_side(const double* __restrict__ in, size
 }
 
 // Faces whose exact solve is still iterating at a pass's cap, with their
-// Newton state, for the next pass.
+// Newton state, for the next pass.  nreg regions of `stride` entries each (the
+// first pass sorts the faces into one region per wave pattern), count[r] the
+// entries of region r.
 struct MfQueue {
     int* face;
     double* p;
-    int* it;
+    int* it;  // iterations done | wave pattern << 16
     int* count;
+    int nreg;
+    size_t stride;
 };
 
-// Iteration caps of the passes.  Most faces converge in under ten Newton
-// iterations, but about one in a hundred random faces never reaches the
-// absolute tolerance and runs the reference's full 500: in one pass a warp
-// would wait for its slowest face, so each pass stops at its cap and queues the
-// unfinished faces, which the next pass resumes side by side.
-constexpr int MF_CAPS[3] = {12, 64, 500};
+// Iteration caps of the passes.  The first pass (cap 0) completes the uniform
+// pairs and sorts every other face by its wave pattern (1-wave rarefaction or
+// shock, 3-wave rarefaction or shock), so that the next pass runs warps of
+// faces that take the same branches: a warp pays each FP64 instruction in full
+// whatever the number of its lanes on that path.  Most faces then converge in
+// under ten Newton iterations, but about one in a hundred random faces never
+// reaches the absolute tolerance and runs the reference's full 500: in one
+// pass a warp would wait for its slowest face, so each pass stops at its cap
+// and queues the unfinished faces, which the next pass resumes side by side.
+constexpr int MF_NPASS = 5;
+constexpr int MF_CAPS[MF_NPASS] = {0, 6, 16, 64, 500};
+constexpr int MF_NREG = 4;  // wave patterns
+constexpr int MF_NCOUNT = MF_NREG + (MF_NPASS - 2);  // queue counts of all passes but the last
 
 // One face: load, rotate into the face frame (:172-189; the scalars are not
 // rotated), solve, assemble.  Returns true when the solve was stopped at cap
@@ -147,21 +158,32 @@ __global__ void __launch_bounds__(128) k_grp2d_flux_mf(int nface, const double* 
 {
     const size_t nf = (size_t)nface;
     const bool resume = qin.face != nullptr;
-    const size_t n = resume ? (size_t)*qin.count : nf;
+    // the input regions, concatenated: entry q of the pass is entry q - start[r] of region r
+    size_t start[MF_NREG + 1];
+    start[0] = 0;
+    for (int r = 0; r < MF_NREG; ++r)
+        start[r + 1] = start[r] + ((resume && r < qin.nreg) ? (size_t)qin.count[r] : 0);
+    const size_t n = resume ? start[MF_NREG] : nf;
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-        MfNewton NW = {0.0, 0};
+        MfNewton NW = {0.0, 0, 0};
         size_t f = q;
         if (resume) {
-            f = (size_t)qin.face[q];
-            NW.p = qin.p[q];
-            NW.it = qin.it[q];
+            int r = 0;
+            while (q >= start[r + 1])
+                ++r;
+            const size_t e = (size_t)r * qin.stride + (q - start[r]);
+            f = (size_t)qin.face[e];
+            NW.p = qin.p[e];
+            NW.it = qin.it[e] & 0xffff;
+            NW.crw = qin.it[e] >> 16;
         }
         // (no face stops in the last pass: its cap is the reference's limit)
         if (mf_face(in, nf, f, P, out, status, bad, cap, resume, NW) && qout.face) {
-            const int slot = atomicAdd(qout.count, 1);
-            qout.face[slot] = (int)f;
-            qout.p[slot] = NW.p;
-            qout.it[slot] = NW.it;
+            const int r = qout.nreg > 1 ? (NW.crw & 3) : 0;
+            const size_t e = (size_t)r * qout.stride + (size_t)atomicAdd(qout.count + r, 1);
+            qout.face[e] = (int)f;
+            qout.p[e] = NW.p;
+            qout.it[e] = NW.it | NW.crw << 16;
         }
     }
 }
@@ -174,8 +196,8 @@ struct MfBuffers {
     double* in = nullptr;
     double* out = nullptr;
     int* status = nullptr;
-    int* bad = nullptr;     // [2] failing-face count and first index, [2..4] queue counts
-    MfQueue q[2] = {};      // ping-pong queues of unfinished faces
+    int* bad = nullptr;     // failing-face count, first index, faces left by each pass
+    MfQueue q[2] = {};      // alternating queues of unfinished faces (face, p, it arrays only)
     size_t cap = 0;  // faces
 
     bool ensure(size_t n)
@@ -183,9 +205,7 @@ struct MfBuffers {
         if (!stream) {
             if (!cuda_ok(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream")) return false;
             if (!cuda_ok(cudaEventCreate(&ev[0]), "event") || !cuda_ok(cudaEventCreate(&ev[1]), "event")) return false;
-            if (!cuda_ok(cudaMalloc(&bad, 4 * sizeof(int)), "alloc")) return false;
-            q[0].count = bad + 2;
-            q[1].count = bad + 3;
+            if (!cuda_ok(cudaMalloc(&bad, (2 + MF_NCOUNT) * sizeof(int)), "alloc")) return false;
         }
         if (n <= cap)
             return true;
@@ -206,11 +226,14 @@ struct MfBuffers {
             !cuda_ok(cudaMalloc(&out, sizeof(double) * MF_NOUT * n), "alloc fluxes") ||
             !cuda_ok(cudaMalloc(&status, sizeof(int) * n), "alloc status"))
             return false;
-        for (auto& Q : q)
-            if (!cuda_ok(cudaMalloc(&Q.face, sizeof(int) * n), "alloc queue") ||
-                !cuda_ok(cudaMalloc(&Q.p, sizeof(double) * n), "alloc queue") ||
-                !cuda_ok(cudaMalloc(&Q.it, sizeof(int) * n), "alloc queue"))
+        // q[0] receives the first pass's faces in one region per wave pattern
+        for (int k = 0; k < 2; ++k) {
+            const size_t entries = (k == 0 ? MF_NREG : 1) * n;
+            if (!cuda_ok(cudaMalloc(&q[k].face, sizeof(int) * entries), "alloc queue") ||
+                !cuda_ok(cudaMalloc(&q[k].p, sizeof(double) * entries), "alloc queue") ||
+                !cuda_ok(cudaMalloc(&q[k].it, sizeof(int) * entries), "alloc queue"))
                 return false;
+        }
         cap = n;
         return true;
     }
@@ -222,8 +245,10 @@ static MfBuffers& mf_buffers()
     return b;
 }
 
-// The passes of one batch on stream s; bad[0..3] must hold {0, INT_MAX, 0, 0}
-// (bad[2], bad[3] are the counts of q[0], q[1]).
+// The passes of one batch on stream s; bad[0 .. 1 + MF_NCOUNT] must hold
+// {0, INT_MAX, 0, ...}: failing faces, first failing index, then the number of
+// faces the first pass queues per wave pattern and each later pass but the
+// last leaves to the next.
 static int launch_grp2d_flux_mf(int nface, const double* d_in, double* d_out, int* d_status, const MfParams& P,
                                 int* d_bad, MfQueue q[2], cudaStream_t s)
 {
@@ -234,10 +259,20 @@ static int launch_grp2d_flux_mf(int nface, const double* d_in, double* d_out, in
     const long long blocks_needed = ((long long)nface + 127) / 128;
     const long long gcap = (long long)sms * 16;
     const int grid = (int)(blocks_needed < gcap ? blocks_needed : gcap);
-    const MfQueue none = {nullptr, nullptr, nullptr, nullptr};
-    for (int pass = 0; pass < 3; ++pass) {
-        const MfQueue& qin = pass == 0 ? none : q[(pass - 1) & 1];
-        const MfQueue& qout = pass == 2 ? none : q[pass & 1];
+    const MfQueue none = {nullptr, nullptr, nullptr, nullptr, 0, 0};
+    // the queue arrays alternate; each pass's output counts have their own
+    // slots after d_bad[0..1] (MF_NREG for the first pass, one for each later
+    // one), so nothing needs resetting between passes
+    auto queue_of = [&](int pass) {
+        MfQueue r = q[pass & 1];
+        r.nreg = pass == 0 ? MF_NREG : 1;
+        r.stride = (size_t)nface;
+        r.count = d_bad + 2 + (pass == 0 ? 0 : MF_NREG + pass - 1);
+        return r;
+    };
+    for (int pass = 0; pass < MF_NPASS; ++pass) {
+        const MfQueue qin = pass == 0 ? none : queue_of(pass - 1);
+        const MfQueue qout = pass == MF_NPASS - 1 ? none : queue_of(pass);
         k_grp2d_flux_mf<<<grid, 128, 0, s>>>(nface, d_in, d_out, d_status, P, d_bad, qin, qout, MF_CAPS[pass]);
         count_launch();
         if (!cuda_ok(cudaGetLastError(), "k_grp2d_flux_mf"))
@@ -278,7 +313,7 @@ extern "C" int hydro_grp2d_flux_mf(int nface, const double* in, double* out, int
     if (!B.ensure((size_t)nface))
         return -1;
     const size_t nf = (size_t)nface;
-    const int init_bad[4] = {0, 0x7fffffff, 0, 0};
+    int init_bad[2 + MF_NCOUNT] = {0, 0x7fffffff};
     if (!cuda_ok(cudaMemcpyAsync(B.bad, init_bad, sizeof(init_bad), cudaMemcpyHostToDevice, B.stream), "upload") ||
         !cuda_ok(cudaMemcpyAsync(B.in, in, sizeof(double) * MF_NIN * nf, cudaMemcpyHostToDevice, B.stream), "upload"))
         return -1;
@@ -286,7 +321,7 @@ extern "C" int hydro_grp2d_flux_mf(int nface, const double* in, double* out, int
     if (launch_grp2d_flux_mf(nface, B.in, B.out, B.status, P, B.bad, B.q, B.stream))
         return -1;
     cudaEventRecord(B.ev[1], B.stream);
-    int bad[4] = {0, 0, 0, 0};
+    int bad[2 + MF_NCOUNT] = {0};
     if (!cuda_ok(cudaMemcpyAsync(out, B.out, sizeof(double) * MF_NOUT * nf, cudaMemcpyDeviceToHost, B.stream),
                  "download") ||
         !cuda_ok(cudaMemcpyAsync(status, B.status, sizeof(int) * nf, cudaMemcpyDeviceToHost, B.stream), "download") ||
@@ -300,8 +335,11 @@ extern "C" int hydro_grp2d_flux_mf(int nface, const double* in, double* out, int
         info->n_bad = bad[0];
         info->first_bad = bad[0] ? bad[1] : -1;
         info->first_code = bad[0] ? status[bad[1]] : 0;
-        info->resumed[0] = bad[2];
-        info->resumed[1] = bad[3];
+        info->resumed[0] = 0;
+        for (int r = 0; r < MF_NREG; ++r)
+            info->resumed[0] += bad[2 + r];
+        for (int k = 1; k < MF_NPASS - 1; ++k)
+            info->resumed[k] = bad[2 + MF_NREG + k - 1];
     }
     return 0;
 }

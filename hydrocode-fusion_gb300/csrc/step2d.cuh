@@ -233,7 +233,7 @@ static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, c
     Star<double> S;
     StarInfo st;
     st.fallback = 0;
-    q1d_star<double, 0, RS>(Ld, Rd, G, S, st, -1.0);
+    q1d_star<double, 0, RS, false>(Ld, Rd, G, S, st, -1.0);
     double D[4], U[4];
     q1d_derivs<double, 0, RS>(Ld, Rd, G, S, D, U);
     const int bad = star_dire_check2(U, D, eps) ? 2 : (ifvar_bad(Ld, Rd, eps) ? 1 : 0);

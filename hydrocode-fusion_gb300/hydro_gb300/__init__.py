@@ -75,7 +75,7 @@ class FaceInfo(ctypes.Structure):
         ("n_bad", ctypes.c_int),
         ("first_bad", ctypes.c_int),
         ("first_code", ctypes.c_int),
-        ("resumed", ctypes.c_int * 2),
+        ("resumed", ctypes.c_int * 4),
         ("kernel_ms", ctypes.c_double),
     ]
 

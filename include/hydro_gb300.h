@@ -285,7 +285,8 @@ typedef struct {
     int n_bad;          /* faces with a non-zero status */
     int first_bad;      /* smallest such face index, -1 if none */
     int first_code;     /* its status */
-    int resumed[2];     /* faces whose Newton iteration went on in the second / third pass */
+    int resumed[4];     /* faces taken up by the 2nd..5th pass (the 1st completes the uniform pairs and
+                           queues the rest; each later one stops at an iteration cap) */
     double kernel_ms;   /* device time of the flux kernels */
 } hydro_face_info;
 int hydro_grp2d_flux_mf(int nface, const double *in, double *out, int *status, const double *cfg, int ncfg,
