@@ -33,3 +33,23 @@ def test_library_exports_declared_symbols():
     assert not missing, missing
     # the configuration array the reference's drivers define is resolvable too
     ctypes.c_double.in_dll(lib, "config")
+
+
+def test_face_flux_argument_checks_need_no_gpu():
+    """hydro_grp2d_flux_mf validates its arguments before any CUDA call: a
+    negative count is rejected (-2), an empty batch succeeds with nothing to
+    report, missing arrays for a non-empty batch are rejected."""
+    import numpy as np
+
+    import hydro_gb300 as hg
+
+    if not os.path.exists(hg.LIB_PATH):
+        hg.build()
+    L = hg.lib()
+    cfg = np.full(400, np.inf)
+    info = hg.FaceInfo()
+    dummy = np.zeros(40)
+    assert L.hydro_grp2d_flux_mf(-1, dummy, dummy, None, cfg, len(cfg), 1e-3, ctypes.byref(info)) == -2
+    assert L.hydro_grp2d_flux_mf(0, dummy, dummy, None, cfg, len(cfg), 1e-3, ctypes.byref(info)) == 0
+    assert info.n_bad == 0 and info.first_bad == -1
+    assert L.hydro_grp2d_flux_mf(5, dummy, dummy, None, cfg, len(cfg), 1e-3, ctypes.byref(info)) == -2
