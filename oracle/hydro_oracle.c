@@ -2692,6 +2692,9 @@ static void scal_from(orc_scal *x, const double *a)
 void orc_grp2d_flux_mf(int cnt, const double *in, double tau, double eps, double gamma_a, double gamma_b,
                        int store_gamma, double *out)
 {
+    /* independent faces: split over the OpenMP threads (the reference's
+       unstructured solver loops over its faces the same way) */
+#pragma omp parallel for schedule(dynamic, 256)
     for (int q = 0; q < cnt; ++q) {
         const double *a = in + 40 * q;
         const double n_x = a[0], n_y = a[1];
