@@ -45,11 +45,17 @@ def test_face_flux_argument_checks_need_no_gpu():
 
     if not os.path.exists(hg.LIB_PATH):
         hg.build()
-    L = hg.lib()
+    # a private handle (RTLD_LOCAL): hg.lib() loads the library globally, and its
+    # config[] would then stand in for the reference harness's own in later tests
+    L = ctypes.CDLL(hg.LIB_PATH)
+    L.hydro_grp2d_flux_mf.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int, ctypes.c_double, ctypes.POINTER(hg.FaceInfo)]
+    L.hydro_grp2d_flux_mf.restype = ctypes.c_int
     cfg = np.full(400, np.inf)
     info = hg.FaceInfo()
     dummy = np.zeros(40)
-    assert L.hydro_grp2d_flux_mf(-1, dummy, dummy, None, cfg, len(cfg), 1e-3, ctypes.byref(info)) == -2
-    assert L.hydro_grp2d_flux_mf(0, dummy, dummy, None, cfg, len(cfg), 1e-3, ctypes.byref(info)) == 0
+    d, c = dummy.ctypes.data, cfg.ctypes.data
+    assert L.hydro_grp2d_flux_mf(-1, d, d, None, c, len(cfg), 1e-3, ctypes.byref(info)) == -2
+    assert L.hydro_grp2d_flux_mf(0, d, d, None, c, len(cfg), 1e-3, ctypes.byref(info)) == 0
     assert info.n_bad == 0 and info.first_bad == -1
-    assert L.hydro_grp2d_flux_mf(5, dummy, dummy, None, cfg, len(cfg), 1e-3, ctypes.byref(info)) == -2
+    assert L.hydro_grp2d_flux_mf(5, d, d, None, c, len(cfg), 1e-3, ctypes.byref(info)) == -2
