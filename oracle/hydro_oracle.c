@@ -12,7 +12,7 @@
  * tests/golden/).  Function-level citations name the reference file:line each
  * routine follows.
  *
- * Deliberate difference (documented in the design doc): when the star-state /
+ * Deliberate difference: when the star-state /
  * time-derivative check of an interface fails, the reference returns before
  * writing that interface's flux and leaves whatever the previous interface on
  * the same OpenMP thread produced; here the flux is still assembled from the
