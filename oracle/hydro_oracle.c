@@ -3,7 +3,7 @@
  *
  * A CPU restatement, in plain C99 + OpenMP, of HydroCODE's Eulerian
  * Godunov/GRP finite-volume step for the 1D and 2D structured single-fluid
- * ideal-gas solver.  It is the checker of the CUDA path (tests/, smoke() and
+ * ideal-gas solver.  The CUDA path is tested against it (tests/, smoke() and
  * bench.py's cpu_baseline only) and never part of the product.
  *
  * Every floating-point expression keeps the reference's operand order, so the

@@ -2,8 +2,8 @@
  * hydro_oracle.h -- TEST INFRASTRUCTURE ONLY.
  *
  * CPU restatement of HydroCODE's Eulerian Godunov/GRP step (1D and 2D
- * structured, single-fluid, ideal gas), used as the checker for the CUDA
- * path and as the timed CPU baseline ("port").  It is pinned against the
+ * structured, single-fluid, ideal gas) that the CUDA path is tested
+ * against, and the timed CPU baseline ("port").  It is pinned against the
  * reference itself (oracle/_ref, built by oracle/Makefile) and against the
  * golden fixtures in tests/golden/.  Nothing in the product links it.
  *

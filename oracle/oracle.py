@@ -8,7 +8,7 @@ Two interchangeable back ends with identical entry points:
                    compiled by ``make -C oracle ref`` where the reference tree
                    exists (this is what pins the port).
 
-Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+Only tests/, the smoke test and bench.py's CPU-baseline leg use
 this module; the product never imports it.
 """
 from __future__ import annotations
