@@ -381,11 +381,15 @@ def mf_suite(hg, peak, nface=8 << 20, reps=5, cpu=True):
     cfg = np.full(400, np.inf)
     cfg[4], cfg[6], cfg[60], cfg[106] = 1e-9, 1.4, 1.0, 3.0
     tau = 1e-4
-    hg.grp2d_flux_mf(f, tau, cfg)   # warm-up: buffers, module load
+    # the caller's output arrays, filled by every call (the warm-up call also
+    # takes their first-touch page faults, and the device buffers, module load)
+    out = np.empty((18, nface))
+    status = np.empty(nface, np.int32)
+    hg.grp2d_flux_mf(f, tau, cfg, out, status)
     kern, wall = [], []
     for _ in range(reps):
         t0 = time.perf_counter()
-        out, status, info = hg.grp2d_flux_mf(f, tau, cfg)
+        out, status, info = hg.grp2d_flux_mf(f, tau, cfg, out, status)
         wall.append(time.perf_counter() - t0)
         kern.append(info.kernel_ms)
     k_ms = float(np.median(kern))

@@ -281,6 +281,46 @@ static int launch_grp2d_flux_mf(int nface, const double* d_in, double* d_out, in
     return 0;
 }
 
+// Device to host copy of `bytes` into the caller's (pageable) memory through
+// the pinned staging pair: each 64 MB block lands in a pinned buffer while host
+// threads move the previous block into place (a pageable copy goes through the
+// driver's own staging at a fraction of the link's speed).
+static int download_staged(void* dst, const void* src, size_t bytes, cudaStream_t s)
+{
+    HostPair* hp = host_pair();
+    if (!hp)
+        return -1;
+    std::lock_guard<std::mutex> guard(hp->lock);
+    const size_t CH = hp->bytes;
+    const size_t nchunk = (bytes + CH - 1) / CH;
+    auto issue = [&](size_t c) -> bool {
+        const size_t off = c * CH, len = bytes - off < CH ? bytes - off : CH;
+        return cuda_ok(cudaMemcpyAsync(hp->buf[c & 1], static_cast<const char*>(src) + off, len,
+                                       cudaMemcpyDeviceToHost, s),
+                       "download") &&
+               cuda_ok(cudaEventRecord(hp->ev[c & 1], s), "staging event");
+    };
+    if (nchunk == 0)
+        return 0;
+    if (!issue(0))
+        return -1;
+    for (size_t c = 0; c < nchunk; ++c) {
+        if (c + 1 < nchunk && !issue(c + 1))
+            return -1;
+        if (!cuda_ok(cudaEventSynchronize(hp->ev[c & 1]), "download wait"))
+            return -1;
+        const size_t off = c * CH, len = bytes - off < CH ? bytes - off : CH;
+        const char* from = static_cast<const char*>(hp->buf[c & 1]);
+        char* to = static_cast<char*>(dst) + off;
+        const int parts = 64;
+        parallel_range(parts, len, [&](int r0, int r1) {
+            const size_t a = len * (size_t)r0 / parts, b = len * (size_t)r1 / parts;
+            memcpy(to + a, from + a, b - a);
+        });
+    }
+    return 0;
+}
+
 }  // namespace hydro
 
 using namespace hydro;
@@ -322,9 +362,8 @@ extern "C" int hydro_grp2d_flux_mf(int nface, const double* in, double* out, int
         return -1;
     cudaEventRecord(B.ev[1], B.stream);
     int bad[2 + MF_NCOUNT] = {0};
-    if (!cuda_ok(cudaMemcpyAsync(out, B.out, sizeof(double) * MF_NOUT * nf, cudaMemcpyDeviceToHost, B.stream),
-                 "download") ||
-        !cuda_ok(cudaMemcpyAsync(status, B.status, sizeof(int) * nf, cudaMemcpyDeviceToHost, B.stream), "download") ||
+    if (download_staged(out, B.out, sizeof(double) * MF_NOUT * nf, B.stream) ||
+        download_staged(status, B.status, sizeof(int) * nf, B.stream) ||
         !cuda_ok(cudaMemcpyAsync(bad, B.bad, sizeof(bad), cudaMemcpyDeviceToHost, B.stream), "download") ||
         !cuda_ok(cudaStreamSynchronize(B.stream), "flux sync"))
         return -1;

@@ -298,18 +298,25 @@ MF_OUT_FIELDS = ("F_rho", "F_u", "F_v", "F_e", "RHO_int", "U_int", "V_int", "P_i
                  "PHI", "Z_a", "U_qt_add_c", "V_qt_add_c", "U_qt_star", "V_qt_star", "P_star")
 
 
-def grp2d_flux_mf(fields, tau, cfg):
+def grp2d_flux_mf(fields, tau, cfg, out=None, status=None):
     """Two-component GRP_2D_flux for a batch of faces on the GPU.
     fields: (40, nface) float64 -- n_x, n_y, then MF_SIDE_FIELDS for the left
     and the right side.  cfg: config[] (4 eps, 6 / 106 the two gammas, 60
-    store F_gamma).  Returns (out (18, nface) in MF_OUT_FIELDS order,
-    status (nface,) int32, FaceInfo)."""
+    store F_gamma).  out (18, nface) float64 and status (nface,) int32 may be
+    given to be filled (a caller that flushes batches repeatedly keeps them).
+    Returns (out in MF_OUT_FIELDS order, status, FaceInfo)."""
     fields = np.ascontiguousarray(fields, np.float64)
     if fields.ndim != 2 or fields.shape[0] != 40:
         raise ValueError("fields must have shape (40, nface)")
     nface = fields.shape[1]
-    out = np.zeros((18, nface))
-    status = np.zeros(nface, np.int32)
+    if out is None:
+        out = np.zeros((18, nface))
+    if status is None:
+        status = np.zeros(nface, np.int32)
+    if out.shape != (18, nface) or out.dtype != np.float64 or not out.flags.c_contiguous:
+        raise ValueError("out must be a C-contiguous float64 array of shape (18, nface)")
+    if status.shape != (nface,) or status.dtype != np.int32 or not status.flags.c_contiguous:
+        raise ValueError("status must be a C-contiguous int32 array of shape (nface,)")
     cfg = np.ascontiguousarray(cfg, np.float64)
     info = FaceInfo()
     rc = lib().hydro_grp2d_flux_mf(nface, fields, out, status.ctypes.data_as(ctypes.c_void_p), cfg, len(cfg),
