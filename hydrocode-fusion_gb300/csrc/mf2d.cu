@@ -321,6 +321,37 @@ static int download_staged(void* dst, const void* src, size_t bytes, cudaStream_
     return 0;
 }
 
+// Host to device copy of `bytes` from the caller's (pageable) memory through
+// the pinned staging pair: host threads fill one pinned buffer while the other
+// is on its way to the device.  A buffer is refilled only after its previous
+// copy has completed (its event).
+static int upload_staged(void* dst, const void* src, size_t bytes, cudaStream_t s)
+{
+    HostPair* hp = host_pair();
+    if (!hp)
+        return -1;
+    std::lock_guard<std::mutex> guard(hp->lock);
+    const size_t CH = hp->bytes;
+    const size_t nchunk = (bytes + CH - 1) / CH;
+    for (size_t c = 0; c < nchunk; ++c) {
+        const size_t off = c * CH, len = bytes - off < CH ? bytes - off : CH;
+        if (c >= 2 && !cuda_ok(cudaEventSynchronize(hp->ev[c & 1]), "upload wait"))
+            return -1;
+        char* to = static_cast<char*>(hp->buf[c & 1]);
+        const char* from = static_cast<const char*>(src) + off;
+        const int parts = 64;
+        parallel_range(parts, len, [&](int r0, int r1) {
+            const size_t a = len * (size_t)r0 / parts, b = len * (size_t)r1 / parts;
+            memcpy(to + a, from + a, b - a);
+        });
+        if (!cuda_ok(cudaMemcpyAsync(static_cast<char*>(dst) + off, to, len, cudaMemcpyHostToDevice, s), "upload") ||
+            !cuda_ok(cudaEventRecord(hp->ev[c & 1], s), "staging event"))
+            return -1;
+    }
+    // the buffers are free again once the last copies are done
+    return cuda_ok(cudaStreamSynchronize(s), "upload sync") ? 0 : -1;
+}
+
 }  // namespace hydro
 
 using namespace hydro;
@@ -355,7 +386,7 @@ extern "C" int hydro_grp2d_flux_mf(int nface, const double* in, double* out, int
     const size_t nf = (size_t)nface;
     int init_bad[2 + MF_NCOUNT] = {0, 0x7fffffff};
     if (!cuda_ok(cudaMemcpyAsync(B.bad, init_bad, sizeof(init_bad), cudaMemcpyHostToDevice, B.stream), "upload") ||
-        !cuda_ok(cudaMemcpyAsync(B.in, in, sizeof(double) * MF_NIN * nf, cudaMemcpyHostToDevice, B.stream), "upload"))
+        upload_staged(B.in, in, sizeof(double) * MF_NIN * nf, B.stream))
         return -1;
     cudaEventRecord(B.ev[0], B.stream);
     if (launch_grp2d_flux_mf(nface, B.in, B.out, B.status, P, B.bad, B.q, B.stream))
