@@ -10,6 +10,8 @@
 #include <string.h>
 
 #include <atomic>
+#include <condition_variable>
+#include <mutex>
 #include <thread>
 #include <string>
 #include <vector>
@@ -217,22 +219,79 @@ static Solver2DBase* make_solver(int m, int n, int form, int rs)
     }
 }
 
+// Worker threads of parallel_range, started on first use and kept for the
+// life of the process (the staged copies call it once per 64 MB block, and
+// starting fifteen threads per call showed up in their times).  One job at a
+// time: callers are serialised, and a job ends when every worker has seen it.
+namespace {
+struct RangePool {
+    std::mutex call;  // one job at a time
+    std::mutex m;
+    std::condition_variable go, done;
+    const std::function<void(int, int)>* fn = nullptr;
+    int rows = 0, T = 0, pending = 0;
+    unsigned gen = 0;
+    int nworkers = 0;
+
+    explicit RangePool(int n) : nworkers(n)
+    {
+        for (int t = 1; t <= n; ++t)
+            std::thread([this, t] { work(t); }).detach();
+    }
+    void work(int t)
+    {
+        unsigned seen = 0;
+        for (;;) {
+            const std::function<void(int, int)>* f;
+            int r, TT;
+            {
+                std::unique_lock<std::mutex> lk(m);
+                go.wait(lk, [&] { return gen != seen; });
+                seen = gen;
+                f = fn;
+                r = rows;
+                TT = T;
+            }
+            if (t < TT)
+                (*f)((int)((long long)r * t / TT), (int)((long long)r * (t + 1) / TT));
+            std::lock_guard<std::mutex> lk(m);
+            if (--pending == 0)
+                done.notify_one();
+        }
+    }
+    void run(int r, int TT, const std::function<void(int, int)>& f)
+    {
+        std::lock_guard<std::mutex> one(call);
+        {
+            std::lock_guard<std::mutex> lk(m);
+            fn = &f;
+            rows = r;
+            T = TT;
+            pending = nworkers;
+            ++gen;
+        }
+        go.notify_all();
+        f(0, (int)((long long)r / TT));
+        std::unique_lock<std::mutex> lk(m);
+        done.wait(lk, [&] { return pending == 0; });
+    }
+};
+}  // namespace
+
 void parallel_range(int rows, size_t bytes, const std::function<void(int, int)>& fn)
 {
     unsigned hw = std::thread::hardware_concurrency();
-    int T = bytes < (size_t)(8u << 20) ? 1 : (int)(hw ? (hw < 16 ? hw : 16) : 4);
+    const int TMAX = (int)(hw ? (hw < 16 ? hw : 16) : 4);
+    int T = bytes < (size_t)(8u << 20) ? 1 : TMAX;
     if (T > rows)
         T = rows;
     if (T <= 1) {
         fn(0, rows);
         return;
     }
-    std::vector<std::thread> th;
-    for (int t = 1; t < T; ++t)
-        th.emplace_back([&, t] { fn((int)((long long)rows * t / T), (int)((long long)rows * (t + 1) / T)); });
-    fn(0, (int)((long long)rows / T));
-    for (auto& x : th)
-        x.join();
+    // never destroyed: its workers wait for jobs until the process ends
+    static RangePool* pool = new RangePool(TMAX - 1);
+    pool->run(rows, T, fn);
 }
 
 // Runs fn(j0, j1) over row blocks of an m x n host copy of the 5 state planes
