@@ -27,14 +27,26 @@
 #include <stdint.h>
 
 #include "hydro_pow.cuh"
+#include "libm_pow.cuh"
+
+// FP64 pow: by default the C library's method (libm_pow.cuh), so that the
+// parity form rounds every pow as the reference does; compiled with
+// -DHYDRO_POW_CR=1, the correctly rounded double-double pow (hydro_pow.cuh),
+// kept for comparison.
+#ifndef HYDRO_POW_CR
+#define HYDRO_POW_CR 0
+#endif
 
 namespace hydro {
 
 template <typename R> struct M;
 template <> struct M<double> {
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-    // double-double pow: agrees with a correctly rounded pow (hydro_pow.cuh)
+#if HYDRO_POW_CR
     static __device__ __forceinline__ double pow_(double x, double y) { return dd_pow(x, y); }
+#else
+    static __device__ __forceinline__ double pow_(double x, double y) { return lpow(x, y); }
+#endif
     static __device__ __forceinline__ double abs_(double x) { return fabs(x); }
     static __device__ __forceinline__ double log_(double x) { return log(x); }
     static __device__ __forceinline__ bool finite_(double x)
@@ -297,10 +309,17 @@ __device__ __forceinline__ R slope_right(R pp, R pR, R cR, const Gas<R>& G)
 }
 
 // Powers of one base x with the logarithm computed once: pow(y) equals
-// M<R>::pow_(x, y) bit for bit (for FP64 it is dd_pow's own path after its
+// M<R>::pow_(x, y) bit for bit (for FP64 it is the pow's own path after its
 // logarithm).  The wave curve of a rarefaction side and the curve's slope need
 // x^mu and x^nu of the same pressure ratio.
 template <typename R> struct PowBase;
+#if !HYDRO_POW_CR
+template <> struct PowBase<double> {
+    LpowBase b;
+    __device__ __forceinline__ void init(double x) { b.init(x); }
+    __device__ __forceinline__ double pow(double y) const { return b.pow_y(y); }
+};
+#else
 template <> struct PowBase<double> {
     double x, lh, ll;
     bool dd;  // x in (0, inf): the double-double path of dd_pow
@@ -325,6 +344,7 @@ template <> struct PowBase<double> {
         return dd_exp(th, tl);
     }
 };
+#endif
 template <> struct PowBase<float> {
     float l2;
     __device__ __forceinline__ void init(float x) { l2 = __log2f(x); }

@@ -15,7 +15,7 @@
 // Phases are separated by cluster barriers; the CFL minimum and the
 // abort/stop flags are reduced per CTA and across the cluster through
 // distributed shared memory.  Compiled with --fmad=false: FP64 operations
-// round as the reference's C code (pow is the correctly rounded dd_pow).
+// round as the reference's C code (pow is the C library's method, libm_pow.cuh).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math.h>

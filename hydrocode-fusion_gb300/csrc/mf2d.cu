@@ -8,7 +8,7 @@
 // reference's struct i_f_var members (src/include/var_struc.h:116-142).
 //
 // Compiled with --fmad=false: the FP64 arithmetic rounds as the reference's C
-// code does (pow is the correctly rounded dd_pow of hydro_pow.cuh).
+// code does (pow is the C library's method of libm_pow.cuh).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>

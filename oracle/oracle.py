@@ -23,13 +23,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libhydro_oracle.so")
 CRPOW_SO = os.path.join(HERE, "_build", "libhydro_oracle_crpow.so")
+# the same with the FP64 device path's pow (the C library's method, libm_pow.cuh)
+LPOW_SO = os.path.join(HERE, "_build", "libhydro_oracle_lpow.so")
 REF_SO = os.path.join(HERE, "_ref", "libhydro_ref.so")
 # the reference with GRP_2D_flux calling the genuinely-2D solver (oracle/Makefile)
 REF_G2D_SO = os.path.join(HERE, "_ref", "libhydro_ref_g2d.so")
 # GRP_2D_flux of the reference's two-component build (MULTIFLUID_BASICS)
 REF_MF_SO = os.path.join(HERE, "_ref", "libhydro_ref_mf.so")
-# Where oracle/Makefile finds the reference sources (only needed to build REF_SO).
-REF_TREE = os.environ.get("HYDRO_REFERENCE", "/root/reference")
+# The reference project's tree, from the HYDRO_REFERENCE environment variable;
+# only needed to build REF_SO (and its variants).  Without it the tests that
+# need the reference build skip, and the committed golden fixtures pin the port.
+REF_TREE = os.environ.get("HYDRO_REFERENCE", "")
 NCONF = 400
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -38,7 +42,7 @@ _dbl = ctypes.c_double
 
 
 def reference_available() -> bool:
-    return os.path.isdir(os.path.join(REF_TREE, "src", "finite_volume"))
+    return bool(REF_TREE) and os.path.isdir(os.path.join(REF_TREE, "src", "finite_volume"))
 
 
 def build(ref: bool = False) -> None:
@@ -78,11 +82,11 @@ def default_config_1d(**kw) -> np.ndarray:
 class Oracle:
     def __init__(self, which: str = "port"):
         """which: "port" (the C restatement), "crpow" (the same with a correctly
-        rounded pow), "reference" (the reference's own sources) or
+        rounded pow), "lpow" (the same with the device path's pow), "reference" (the reference's own sources) or
         "reference_g2d" (the same with GRP_2D_flux calling the genuinely-2D
         solver; the port selects it per run with config[301] = 1) or
         "reference_mf" (only the two-component interface flux, grp2d_flux_mf)."""
-        path = {"port": PORT_SO, "crpow": CRPOW_SO, "reference_g2d": REF_G2D_SO,
+        path = {"port": PORT_SO, "crpow": CRPOW_SO, "lpow": LPOW_SO, "reference_g2d": REF_G2D_SO,
                 "reference_mf": REF_MF_SO}.get(which, REF_SO)
         if not os.path.exists(path):
             raise FileNotFoundError(f"oracle library missing: {path} (run make -C oracle)")

@@ -32,7 +32,7 @@ def ref():
 
     if not os.path.exists(orc.REF_SO):
         if not orc.reference_available():
-            pytest.skip("reference tree not present on this machine")
+            pytest.skip("reference tree not given (set HYDRO_REFERENCE)")
         orc.build(ref=True)
     return orc.Oracle("reference")
 
@@ -45,7 +45,7 @@ def ref_g2d():
 
     if not os.path.exists(orc.REF_G2D_SO):
         if not orc.reference_available():
-            pytest.skip("reference tree not present on this machine")
+            pytest.skip("reference tree not given (set HYDRO_REFERENCE)")
         orc.build(ref=True)
     return orc.Oracle("reference_g2d")
 
@@ -58,7 +58,7 @@ def ref_mf():
 
     if not os.path.exists(orc.REF_MF_SO):
         if not orc.reference_available():
-            pytest.skip("reference tree not present on this machine")
+            pytest.skip("reference tree not given (set HYDRO_REFERENCE)")
         orc.build(ref=True)
     return orc.Oracle("reference_mf")
 
