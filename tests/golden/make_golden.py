@@ -6,7 +6,8 @@ stores inputs and float64 outputs as .npz files.  Only this script needs the
 reference tree; the fixtures travel with the repository.
 
     python tests/golden/make_golden.py            # all fixtures
-    python tests/golden/make_golden.py --large    # also the 1024^2 x 500 run summary
+    python tests/golden/make_golden.py --large    # also the 1024^2 x 100 / x 500 run summaries
+    python tests/golden/make_golden.py --only large  # only those two summaries
     python tests/golden/make_golden.py --only g2d # only the genuinely-2D solver's fixtures
     python tests/golden/make_golden.py --only lag # only the 1D Lagrangian schemes' fixtures
     python tests/golden/make_golden.py --only mf  # only the two-component interface flux
@@ -20,6 +21,7 @@ two-component interface-flux fixture comes from oracle/_ref/libhydro_ref_mf.so
 from __future__ import annotations
 
 import argparse
+import hashlib
 import os
 import sys
 
@@ -232,10 +234,37 @@ def make_lag():
     np.savez_compressed(os.path.join(HERE, "runs_1d_lag.npz"), **r1)
 
 
+def field_sha256(a: np.ndarray) -> str:
+    """SHA-256 of a field's float64 values, little-endian, x-major (C order):
+    the full-field identity of a run, checkable on any host."""
+    return hashlib.sha256(np.ascontiguousarray(a, "<f8").tobytes()).hexdigest()
+
+
+def make_large():
+    """Summaries of the 1024^2 four-quadrant run (transmissive, CFL 0.45) after
+    100 and 500 steps: step count and time, per field its SHA-256, sums, a 64 x 64
+    subsample, one row and one column."""
+    R = orc.Oracle("reference")
+    m = n = 1024
+    rho, u, v, p = cases.four_quadrant(m, n, seed=2024)
+    for steps in (100, 500):
+        cfg = orc.default_config_2d(t_all=-1, steps=steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
+        out = R.run_2d(rho, u, v, p, cfg)
+        summ = {"meta": np.array([out["steps"], out["time"], out["wall"]]), "cfg": cfg}
+        for f in ("rho", "u", "v", "p", "E"):
+            summ[f"sha256/{f}"] = np.array(field_sha256(out[f]))
+            summ[f"abs_sum/{f}"] = np.abs(out[f]).sum()
+            summ[f"sum/{f}"] = out[f].sum()
+            summ[f"sub/{f}"] = out[f][::16, ::16].copy()
+            summ[f"row/{f}"] = out[f][m // 2 + 3, :].copy()
+            summ[f"col/{f}"] = out[f][:, n // 2 - 5].copy()
+        np.savez_compressed(os.path.join(HERE, f"fq1024_{steps}.npz"), **summ)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--large", action="store_true")
-    ap.add_argument("--only", choices=["all", "g2d", "lag", "mf"], default="all")
+    ap.add_argument("--only", choices=["all", "g2d", "lag", "mf", "large"], default="all")
     args = ap.parse_args()
     orc.build(ref=True)
     if args.only in ("all", "g2d"):
@@ -244,6 +273,8 @@ def main():
         make_lag()
     if args.only in ("all", "mf"):
         make_mf()
+    if args.only == "large":
+        make_large()
     if args.only != "all":
         print("fixtures written to", HERE)
         return
@@ -308,19 +339,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "runs_1d.npz"), **r1)
 
     if args.large:
-        m = n = 1024
-        rho, u, v, p = cases.four_quadrant(m, n, seed=2024)
-        for steps in (100, 500):
-            cfg = orc.default_config_2d(t_all=-1, steps=steps, hx=1.0 / m, hy=1.0 / n, bx=-4, by=-4)
-            out = R.run_2d(rho, u, v, p, cfg)
-            summ = {"meta": np.array([out["steps"], out["time"], out["wall"]]), "cfg": cfg}
-            for f in ("rho", "u", "v", "p", "E"):
-                summ[f"abs_sum/{f}"] = np.abs(out[f]).sum()
-                summ[f"sum/{f}"] = out[f].sum()
-                summ[f"sub/{f}"] = out[f][::16, ::16].copy()
-                summ[f"row/{f}"] = out[f][m // 2 + 3, :].copy()
-                summ[f"col/{f}"] = out[f][:, n // 2 - 5].copy()
-            np.savez_compressed(os.path.join(HERE, f"fq1024_{steps}.npz"), **summ)
+        make_large()
     print("fixtures written to", HERE)
 
 

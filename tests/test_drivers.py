@@ -165,13 +165,10 @@ def test_1d_driver_lagrangian_sod(gpu_lib, tmp_path, order):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "Lagrangian scheme" in r.stdout
     out = tmp_path / "data_out" / "one-dim" / f"LAG_{order}_order" / "sod_lag"
-    # the oracle with the device's correctly rounded pow: Sod-GRP in Lagrangian
-    # coordinates amplifies glibc's pow rounding to ~1e-8 in places (see
-    # test_parity_1d_lag.py), more than the text's 10 digits absorb
     import oracle as orc
 
     cfg = orc.default_config_1d(t_all=0.2, steps=100000, hx=0.0025, bx=-4, cfl=0.45)
-    want = orc.Oracle("crpow").run_1d_lag(rho, u, p, cfg, order)
+    want = orc.Oracle("port").run_1d_lag(rho, u, p, cfg, order)
     for name, key in (("RHO", "rho"), ("U", "u"), ("P", "p")):
         got = _read_dat(out / f"{name}.dat")
         np.testing.assert_allclose(got[-1], want[key], rtol=RTOL_TEXT, atol=1e-12)

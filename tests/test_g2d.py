@@ -10,7 +10,7 @@ import pytest
 from helpers import FIELDS, rel_l1
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-TOL = 1e-12   # FP64 form vs the reference (relative L1); only pow rounds differently
+TOL = 1e-12   # FP64 form vs the reference (relative L1)
 FP32_TOL = 2e-5
 
 

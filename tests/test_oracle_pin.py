@@ -1,13 +1,28 @@
 """Pin the oracle (C restatement) to the reference: bit-for-bit against the
 golden fixtures generated from the reference's own sources
 (tests/golden/make_golden.py), against the reference library itself where the
-reference tree exists, and against analytic known answers."""
+reference tree exists, and against analytic known answers.
+
+Every test runs twice: with the oracle as built ("port", which calls this
+host's C library pow, as the reference does) and with its twin whose pow is
+the FP64 device path's (``lpow``: a host build of csrc/libm_pow.cuh).  The
+twin passing every pin bit for bit shows, without a GPU, that the device's pow
+rounds as the reference's does on every argument these runs produce."""
 import os
 
 import numpy as np
 import pytest
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module", params=["port", "lpow"])
+def port(request):
+    import oracle as orc
+
+    if not (os.path.exists(orc.PORT_SO) and os.path.exists(orc.LPOW_SO)):
+        orc.build()
+    return orc.Oracle(request.param)
 
 
 def load(name):

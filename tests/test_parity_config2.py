@@ -1,24 +1,22 @@
 """The headline parity case: 2D unsplit GRP, FP64, 1024 x 1024 seeded
-four-quadrant Riemann data, transmissive boundaries, CFL 0.45.
+four-quadrant Riemann data, transmissive boundaries, CFL 0.45, after 100 and
+after 500 steps, full field.
 
-Every FP64 operation of the device path rounds exactly as the reference's C
-code; the one library function on the path, pow(), is computed correctly
-rounded on the device (csrc/hydro_pow.cuh), while the reference calls glibc's
-pow, whose last bit differs from the correctly rounded value on ~0.06% of the
-arguments.  Those last-bit differences stay at round-off for the first ~100
-steps and are amplified afterwards (Newton stopping test, limiter switches):
+Every FP64 operation of the device path rounds as the reference's C code,
+pow included (csrc/libm_pow.cuh follows the C library's own method).  The
+reference's own runs are pinned by the SHA-256 of each full field
+(tests/golden/fq1024_{100,500}.npz, written by make_golden.py from the
+reference build), so the comparison needs neither the reference tree nor a
+stored 40 MB state:
 
-* 100 steps, against the reference's own run (golden summary): relative L1
-  <= 1e-12 in rho, u, v, p;
-* 500 steps, against the oracle built with a correctly rounded pow
-  (oracle/_build/libhydro_oracle_crpow.so): bit-identical full field -- the
-  device reproduces the reference's arithmetic exactly;
-* 500 steps, against the reference's own run with glibc's pow: full-field
-  relative L1 measured 7.0e-12 in rho (the pow rounding effect above); the
-  golden summary holds a 64 x 64 subsample, the field sums and one row and one
-  column, bounded here by 3e-11 (subsample, sums) and 2e-10 (a single line,
-  where fewer cells average the differences).
+* the device's fields hash to the reference's: the full field is identical in
+  every cell (relative L1 = 0);
+* should a hash differ, the oracle is run on the same input on this host; when
+  its fields hash to the reference's it IS the reference's result, and the
+  device's full fields must be within relative L1 1e-12 of it in rho, u, v
+  and p -- the benchmark spec's bound -- with the step count and time equal.
 """
+import hashlib
 import os
 
 import numpy as np
@@ -28,6 +26,12 @@ from helpers import rel_l1
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 M = 1024
+TOL = 1e-12
+FIELDS = ("rho", "u", "v", "p", "E")
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, "<f8").tobytes()).hexdigest()
 
 
 def _gpu_run(hg, steps):
@@ -39,43 +43,35 @@ def _gpu_run(hg, steps):
     return (rho, u, v, p), cfg, got, info
 
 
-def _against_golden(got, info, d, tol, line_tol=None):
-    """Relative L1 of the 64 x 64 subsample and relative error of the field's
-    L1 norm (<= tol), and relative L1 along one row and one column (<= line_tol)."""
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [100, 500])
+def test_config2_full_field_matches_reference(gpu_lib, steps):
+    d = np.load(os.path.join(GOLD, f"fq1024_{steps}.npz"))
+    (rho, u, v, p), cfg, got, info = _gpu_run(gpu_lib, steps)
     assert info.k_out == int(d["meta"][0]) and info.time == d["meta"][1]
-    line_tol = tol if line_tol is None else line_tol
-    errs = {}
-    for f in ("rho", "u", "v", "p"):
-        errs[f"sub/{f}"] = rel_l1(got[f][::16, ::16], d[f"sub/{f}"])
-        errs[f"abs_sum/{f}"] = abs(np.abs(got[f]).sum() - d[f"abs_sum/{f}"]) / d[f"abs_sum/{f}"]
-        errs[f"row/{f}"] = rel_l1(got[f][M // 2 + 3, :], d[f"row/{f}"])
-        errs[f"col/{f}"] = rel_l1(got[f][:, M // 2 - 5], d[f"col/{f}"])
-    bad = {k: v for k, v in errs.items() if v > (line_tol if k[:3] in ("row", "col") else tol)}
-    assert not bad, errs
-    return errs
-
-
-@pytest.mark.gpu
-def test_config2_100_steps_against_reference(gpu_lib):
-    _, _, got, info = _gpu_run(gpu_lib, 100)
-    _against_golden(got, info, np.load(os.path.join(GOLD, "fq1024_100.npz")), 1e-12)
-
-
-@pytest.mark.gpu
-def test_config2_500_steps_bitexact_with_correctly_rounded_pow(gpu_lib):
+    same = {f: _sha(got[f]) == str(d[f"sha256/{f}"]) for f in FIELDS}
+    if all(same.values()):
+        return
     import oracle as orc
 
-    if not os.path.exists(orc.CRPOW_SO):
+    if not os.path.exists(orc.PORT_SO):
         orc.build()
-    crpow = orc.Oracle("crpow")
-    (rho, u, v, p), cfg, got, info = _gpu_run(gpu_lib, 500)
-    want = crpow.run_2d(rho, u, v, p, cfg)
-    assert info.k_out == int(want["steps"]) and info.time == want["time"]
-    for f in ("rho", "u", "v", "p", "E"):
-        assert np.array_equal(got[f], want[f]), (f, rel_l1(got[f], want[f]))
+    want = orc.Oracle("port").run_2d(rho, u, v, p, cfg)
+    oracle_is_reference = all(_sha(want[f]) == str(d[f"sha256/{f}"]) for f in FIELDS)
+    assert oracle_is_reference, "the oracle on this host does not reproduce the reference's fields"
+    errs = {f: rel_l1(got[f], want[f]) for f in ("rho", "u", "v", "p")}
+    assert all(e <= TOL for e in errs.values()), (same, errs)
 
 
 @pytest.mark.gpu
-def test_config2_500_steps_against_reference(gpu_lib):
-    _, _, got, info = _gpu_run(gpu_lib, 500)
-    _against_golden(got, info, np.load(os.path.join(GOLD, "fq1024_500.npz")), 3e-11, 2e-10)
+def test_config2_summaries_match_reference(gpu_lib):
+    """The 64 x 64 subsample, one row, one column and the field sums of the
+    golden summary at 100 steps (a readable report of where a difference lies,
+    should the full-field test above fail)."""
+    d = np.load(os.path.join(GOLD, "fq1024_100.npz"))
+    _, _, got, info = _gpu_run(gpu_lib, 100)
+    for f in ("rho", "u", "v", "p"):
+        assert rel_l1(got[f][::16, ::16], d[f"sub/{f}"]) <= TOL, f
+        assert rel_l1(got[f][M // 2 + 3, :], d[f"row/{f}"]) <= TOL, f
+        assert rel_l1(got[f][:, M // 2 - 5], d[f"col/{f}"]) <= TOL, f
+        assert abs(np.abs(got[f]).sum() - d[f"abs_sum/{f}"]) <= TOL * d[f"abs_sum/{f}"], f

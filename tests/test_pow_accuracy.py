@@ -1,10 +1,15 @@
-"""The FP64 form's pow (double-double, csrc/hydro_pow.cuh) against the C
-library's pow -- the one the reference calls -- on the arguments the solver
-produces (pressure/sound-speed ratios; the exponents of the exact Riemann
-solver and the GRP for several gammas) and on arbitrary ones.  They agree on
-all but a small fraction, and wherever they disagree the double-double result
-is the correctly rounded one (checked with 60-digit decimal arithmetic): the
-residue is the C library's own last-bit rounding.  Host build of the same code."""
+"""The FP64 form's pow functions against the C library's pow -- the one the
+reference calls -- on the arguments the solver produces (pressure/sound-speed
+ratios; the exponents of the exact Riemann solver and the GRP for several
+gammas) and on arbitrary ones.  Host builds of the device code.
+
+* libm_pow.cuh (the device default) follows the C library's own method and
+  returns the C library's bits: no argument of the solver sample differs, and
+  at most a handful in tens of millions of arbitrary ones.
+* hydro_pow.cuh (correctly rounded double-double pow, kept for comparison)
+  differs from the C library on ~0.06% of the arguments, and wherever they
+  differ it is the correctly rounded one (60-digit decimal arithmetic): the
+  residue is the C library's own last-bit rounding."""
 import ctypes
 import os
 import subprocess
@@ -12,6 +17,7 @@ import tempfile
 from decimal import Decimal, getcontext
 
 import numpy as np
+import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -25,7 +31,69 @@ def _lib():
     dp = np.ctypeslib.ndpointer(np.float64, flags="C")
     L.pow_pair.argtypes = [dp, dp, ctypes.c_longlong, dp, dp]
     L.pow_pair.restype = None
+    L.lpow_pair.argtypes = [dp, dp, ctypes.c_longlong, dp, dp]
+    L.lpow_pair.restype = None
+    L.lpow_shared_log_mismatch.argtypes = [dp, ctypes.c_longlong, ctypes.c_double, ctypes.c_double]
+    L.lpow_shared_log_mismatch.restype = ctypes.c_longlong
     return L
+
+
+def _solver_args(rng, n):
+    exps = []
+    for g in (1.4, 5.0 / 3.0, 1.2, 3.0):
+        zeta = (g - 1.0) / (g + 1.0)
+        exps += [(g - 1.0) / (2.0 * g), (g + 1.0) / (2.0 * g), 1.0 / g, 0.5 * (g - 1.0) / g,
+                 2.0 * g / (g - 1.0), 0.5 / zeta, (1.0 + zeta) / zeta, g / (g - 1.0), 3.0]
+    y = np.array(exps)[rng.integers(0, len(exps), n)]
+    x = np.exp(rng.uniform(np.log(1e-6), np.log(1e6), n))
+    x[: n // 4] = 1.0 + rng.normal(0, 1e-6, n // 4)  # ratios near 1 (Newton near convergence)
+    x[n // 4: n // 2] = 1.0 + rng.normal(0, 5e-3, n // 4)
+    return x, y
+
+
+def _libm_is_the_fma_variant():
+    """The C library's pow computes with fused multiply-adds on AArch64 and on
+    x86-64 processors with FMA (the case the reference's fixtures were made
+    in); elsewhere it takes another variant of the method."""
+    import platform
+    if platform.machine() in ("aarch64", "arm64"):
+        return True
+    try:
+        with open("/proc/cpuinfo") as f:
+            flags = next((ln for ln in f if ln.startswith("flags")), "").split()
+        return "fma" in flags and "avx2" in flags
+    except OSError:
+        return False
+
+
+def test_libm_method_pow_returns_the_c_library_bits():
+    if not _libm_is_the_fma_variant():
+        pytest.skip("this host's C library pow takes its variant without fused multiply-add")
+    L = _lib()
+    rng = np.random.default_rng(11)
+    n = 2_000_000
+    x, y = _solver_args(rng, n)
+    a, b = np.zeros(n), np.zeros(n)
+    L.lpow_pair(x, y, n, a, b)
+    assert np.array_equal(a, b), int((a != b).sum())
+    x, y = np.exp(rng.uniform(-5, 5, n)), rng.uniform(-8, 8, n)
+    L.lpow_pair(x, y, n, a, b)
+    assert (a != b).sum() <= 2, int((a != b).sum())
+    # the solver's whole range of pressure ratios, and subnormal, tiny and huge bases
+    x = np.concatenate([np.exp(rng.uniform(-700, 700, n // 2)), np.ldexp(rng.uniform(0.5, 1, 1000), -1060)])
+    y = np.concatenate([rng.uniform(-0.7, 0.7, n // 2), np.full(1000, 0.2)])
+    a, b = np.zeros(len(x)), np.zeros(len(x))
+    L.lpow_pair(x, y, len(x), a, b)
+    assert (a != b).sum() <= 2, int((a != b).sum())
+
+
+def test_libm_method_pow_shares_one_logarithm():
+    """x^mu and x^nu from one logarithm equal two separate calls bit for bit."""
+    L = _lib()
+    rng = np.random.default_rng(12)
+    x = np.exp(rng.uniform(-10, 10, 500_000))
+    for g in (1.4, 5.0 / 3.0):
+        assert L.lpow_shared_log_mismatch(x, len(x), (g - 1) / (2 * g), (g + 1) / (2 * g)) == 0
 
 
 def _check(L, x, y):
