@@ -16,6 +16,7 @@
 // abort/stop flags are reduced per CTA and across the cluster through
 // distributed shared memory.  Compiled with --fmad=false: FP64 operations
 // round as the reference's C code (pow is the C library's method, libm_pow.cuh).
+#include <atomic>
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -490,10 +491,22 @@ __global__ void __launch_bounds__(512) k_run1d_lag(const __grid_constant__ Run1D
 // launch_run1d in solver1d.cu); halves the cluster when it cannot be placed.
 static cudaError_t launch_run1d_lag(const Run1DLagArgs& a, cudaStream_t st)
 {
-    static int attr_set = -1;
-    if (attr_set < 0) {
-        attr_set = cudaFuncSetAttribute(k_run1d_lag, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
-        cudaGetLastError();
+    // per-device kernel attribute, set on each device's first launch
+    // (0 = not tried, 1 = set, 2 = refused)
+    enum { MAX_DEVICES = 64 };
+    static std::atomic<int> attr_state[MAX_DEVICES];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int attr_set = 0;
+    if (dev >= 0 && dev < MAX_DEVICES) {
+        int st0 = attr_state[dev].load(std::memory_order_acquire);
+        if (st0 == 0) {
+            st0 = cudaFuncSetAttribute(k_run1d_lag, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess
+                      ? 1 : 2;
+            cudaGetLastError();
+            attr_state[dev].store(st0, std::memory_order_release);
+        }
+        attr_set = st0 == 1;
     }
     const int faces = a.m + 1;
     int nt = 32 * ((faces + 32 * 16 - 1) / (32 * 16));

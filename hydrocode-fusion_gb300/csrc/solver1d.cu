@@ -16,6 +16,7 @@
 // with bound_cond_slope_limiter (src/inter_process/bound_cond_slope_limiter.c:30-136)
 // and minmod_limiter (src/inter_process/slope_limiter.c:31-83).  Compiled with
 // --fmad=false: FP64 operations round as the reference's C code.
+#include <atomic>
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -379,10 +380,21 @@ __global__ void __launch_bounds__(512) k_run1d(const __grid_constant__ Run1DArgs
 // so the exact solves of a step spread over up to 16 SMs.
 static cudaError_t launch_run1d(const Run1DArgs& a, cudaStream_t st)
 {
-    static int attr_set = -1;
-    if (attr_set < 0) {
-        attr_set = cudaFuncSetAttribute(k_run1d, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
-        cudaGetLastError();
+    // the non-portable cluster size is a per-device attribute of the kernel:
+    // set it on each device's first launch (0 = not tried, 1 = set, 2 = refused)
+    enum { MAX_DEVICES = 64 };
+    static std::atomic<int> attr_state[MAX_DEVICES];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int attr_set = 0;
+    if (dev >= 0 && dev < MAX_DEVICES) {
+        int st0 = attr_state[dev].load(std::memory_order_acquire);
+        if (st0 == 0) {
+            st0 = cudaFuncSetAttribute(k_run1d, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess ? 1 : 2;
+            cudaGetLastError();
+            attr_state[dev].store(st0, std::memory_order_release);
+        }
+        attr_set = st0 == 1;
     }
     const int faces = a.m + 1;
     int nt = 32 * ((faces + 32 * 16 - 1) / (32 * 16));
@@ -533,10 +545,10 @@ static int run1d(int m, int order, const double* cfg, int ncfg, double* state, c
 // ---------------------------------------------------------------------------
 // Allocation-free variant of the 1D run.
 //
-// Some callers cannot allocate device memory: code that runs while a stream
-// is being captured into a CUDA graph (cudaMalloc is not allowed there),
-// frameworks that own the whole device pool through their own allocator, or
-// embedded drivers whose memory budget is fixed at start-up.  For them the
+// Some callers cannot allocate device memory: frameworks that own the whole
+// device pool through their own allocator (a cudaMalloc behind its back can
+// fail or fragment the pool it has reserved), or embedded drivers whose memory
+// budget is fixed at start-up.  For them the
 // scratch of the 1D kernel (copy of the initial state, one snapshot slot,
 // slopes, interface values, time derivatives, fluxes, result words) lives in
 // the file-scope array below, sized for at most HYDRO1D_NOALLOC_MAX_CELLS
@@ -546,11 +558,12 @@ static int run1d(int m, int order, const double* cfg, int ncfg, double* state, c
 // Host code cannot use the array's name as a device address (it names a
 // host-side stand-in), so the device address is looked up with
 // cudaGetSymbolAddress once per device, on the first call made on that device
-// with that device current; that first call should therefore come before any
-// stream capture.  Every call shares the one array and it keeps the previous
-// call's contents: the slopes and result words are cleared on each call, and
-// calls that overlap on the GPU (several streams, several host threads) race
-// on it, so a caller must serialise them.
+// with that device current, and cached per device.  Every call shares the one
+// array and it keeps the previous call's contents: the slopes and result words
+// are cleared on each call, and calls that overlap on the GPU (several
+// streams, several host threads) race on it, so a caller must serialise them.
+// The call copies its time-plot pair in from and its result words out to host
+// memory and waits for its stream before it returns.
 // ---------------------------------------------------------------------------
 #define HYDRO1D_NOALLOC_MAX_CELLS 16384
 #define HYDRO1D_NOALLOC_DOUBLES (20 * HYDRO1D_NOALLOC_MAX_CELLS + 19)
@@ -560,21 +573,24 @@ static __device__ __align__(256) double g_noalloc_scratch[HYDRO1D_NOALLOC_DOUBLE
 static double* noalloc_scratch_address(int* err)
 {
     enum { MAX_DEVICES = 64 };
-    static double* addr[MAX_DEVICES];
+    static std::atomic<double*> addr[MAX_DEVICES];
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice") || dev < 0 || dev >= MAX_DEVICES) {
         *err = -1;
         return nullptr;
     }
-    if (!addr[dev]) {
+    double* a = addr[dev].load(std::memory_order_acquire);
+    if (!a) {
+        // two host threads may both look it up; they store the same address
         void* p = nullptr;
         if (!cuda_ok(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress")) {
             *err = -1;
             return nullptr;
         }
-        addr[dev] = (double*)p;
+        a = (double*)p;
+        addr[dev].store(a, std::memory_order_release);
     }
-    return addr[dev];
+    return a;
 }
 
 static int run1d_noalloc(int m, double* d_state, const double* cfg, int ncfg, int order, cudaStream_t st,

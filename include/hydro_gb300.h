@@ -155,15 +155,16 @@ int hydro2d_get_variant(hydro2d_t *h, int *shape);
  * NULL) receives one time per variant. */
 int hydro2d_autotune(hydro2d_t *h, const double *cfg, int ncfg, int steps, float *times_ms);
 /* Allocation-free 1D run (no counterpart in the reference): for callers that
- * cannot allocate device memory -- code running while a stream is captured into
- * a CUDA graph, frameworks that own the device pool, drivers with a fixed
- * memory budget.  d_state is the caller's device buffer [4][m] (rho, u, p, E),
- * initial state in, final state out; the scheme's scratch is a fixed static
- * device array of the library (at most 16384 cells; larger m returns -3 with a
- * message).  The first call on a device looks the array up and should come
- * before any stream capture; calls share the array, so overlapping calls race
- * and must be serialised.  stream: a cudaStream_t (NULL = legacy default
- * stream).  Nothing is allocated or freed; the call waits for its stream. */
+ * cannot allocate device memory -- frameworks that own the device pool through
+ * their own allocator, drivers with a fixed memory budget.  d_state is the
+ * caller's device buffer [4][m] (rho, u, p, E), initial state in, final state
+ * out; the scheme's scratch is a fixed static device array of the library
+ * (20 m + 19 doubles for at most 16384 cells, held by every GPU that loads the
+ * library; larger m returns -3 with a message).  The first call on a device
+ * looks the array's address up (cached per device); calls share the array, so
+ * overlapping calls race and must be serialised.  stream: a cudaStream_t
+ * (NULL = legacy default stream).  Nothing is allocated or freed; the call
+ * copies its result words to the host and waits for its stream. */
 int hydro1d_run_noalloc(int m, double *d_state, const double *cfg, int ncfg, int order, void *stream,
                         hydro_run_info *info);
 /* ---- learned Newton starting pressure (no reference counterpart) ---------

@@ -1,8 +1,8 @@
 """The allocation-free 1D entry point (hydro1d_run_noalloc).
 
-It serves callers that cannot allocate device memory (stream capture, an
-allocator that owns the device pool, a fixed memory budget): its scratch is a
-fixed static device array.  The test plays such a caller -- the state buffers
+It serves callers that cannot allocate device memory (a framework whose own
+allocator owns the device pool, a driver with a fixed memory budget): its
+scratch is a fixed static device array.  The test plays such a caller -- the state buffers
 are allocated here, by the test, and only their device addresses cross the C
 ABI -- and checks that two calls in a row give the same results as the
 allocating entry point hydro1d_run, at the parity tolerance of the other tests,
