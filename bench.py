@@ -551,8 +551,9 @@ def main():
     ms = head["ms_per_step"]
     achieved = BYTES_PER_CELL_F32 * m * n / (ms * 1e-3) / 1e9
     kv = head["kernel_variant"]
-    kname = "%s<float,%dx%d,%d,learned>" % ("k_step_tma" if kv.get("tma") else "k_step_unsplit", kv["tile_x"],
-                                             kv["tile_y"], kv["threads"])
+    kname = "%s<float,%dx%d,%d,learned>" % ({"tma": "k_step_tma", "strip": "k_step_strip"}.get(kv.get("kernel"),
+                                                                                           "k_step_unsplit"),
+                                             kv["tile_x"], kv["tile_y"], kv["threads"])
     tpc, tkern = traffic_per_cell("fp32_learned")
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": tpc * m * n if tpc else None, "peak_source": peak_kind,

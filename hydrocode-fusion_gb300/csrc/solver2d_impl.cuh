@@ -21,6 +21,7 @@
 
 #include "solver2d.h"
 #include "step2d.cuh"
+#include "strip2d.cuh"
 
 namespace hydro {
 
@@ -29,7 +30,9 @@ namespace hydro {
 // autotuner (Solver2D::autotune) times them on the actual problem.
 // tma = 1 or 2: the persistent TMA-staged kernel (k_step_tma) with that many
 // shared-memory stages, launched with occ CTAs per SM; tma = 0: one CTA per
-// tile (k_step_unsplit).
+// tile (k_step_unsplit).  strip = 1: the FP32 strip kernel (k_step_strip,
+// strip2d.cuh), persistent with occ CTAs per SM, TJ = rows per work unit,
+// TI = columns a strip updates.
 template <typename R>
 struct StepVariant {
     int TJ, TI, NT, MINB;
@@ -38,6 +41,7 @@ struct StepVariant {
     int tma = 0;
     int occ = 0;
     StepMaps maps[2];  // tma: descriptors of the two state buffers
+    int strip = 0;
 };
 
 template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int RS = 0>
@@ -55,6 +59,15 @@ StepVariant<R> tma_variant()
                           (const void*)k_step_tma<R, TJ, TI, NT, MINB, LEARNED, STAGES, RS>, STAGES, 0, {}};
 }
 
+template <int NW, int MINB, bool LEARNED>
+StepVariant<float> strip_variant(int seg)
+{
+    StepVariant<float> v{seg, STRIP_W, NW * 32, MINB, StripSmem<NW, LEARNED>::bytes,
+                         (const void*)k_step_strip<NW, MINB, LEARNED>, 0, 0, {}};
+    v.strip = 1;
+    return v;
+}
+
 // The compiled configurations, each list instantiated in its own translation
 // unit so the kernels compile in parallel (f32_gathered.cu, f32_tma.cu,
 // f32_learned.cu, f64_variants.cu, g2d_f32.cu, g2d_f64.cu).  The lists keep
@@ -64,6 +77,7 @@ StepVariant<R> tma_variant()
 void variants_f32_gathered(std::vector<StepVariant<float>>& v);
 void variants_f32_tma(std::vector<StepVariant<float>>& v);
 void variants_f32_learned(std::vector<StepVariant<float>>& v);
+void variants_f32_strip(std::vector<StepVariant<float>>& v, bool learned);
 void variants_f64(std::vector<StepVariant<double>>& v);
 void variants_f32_g2d(std::vector<StepVariant<float>>& v);
 void variants_f64_g2d(std::vector<StepVariant<double>>& v);
@@ -89,10 +103,12 @@ template <> struct Variants<float> {
             variants_f32_g2d(v);
         } else if (learned) {
             variants_f32_learned(v);
+            variants_f32_strip(v, true);
         } else {
             // the TMA-staged kernels first: index 0 is the default when nothing is tuned
             variants_f32_tma(v);
             variants_f32_gathered(v);
+            variants_f32_strip(v, false);
         }
         return v;
     }
@@ -294,6 +310,7 @@ public:
     Ctl* ctl = nullptr;
     double* stage = nullptr;   // FP64 staging, 5 planes of m*n
     unsigned long long* red = nullptr;
+    unsigned int* work = nullptr;  // per-launch work counters of the strip kernel
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int sms = 148;
@@ -370,6 +387,7 @@ public:
         if (!cuda_ok(cudaMalloc(&ghost0, sizeof(R) * (8 * (size_t)n + 8 * (size_t)m)), "ghost table")) return -1;
         if (!cuda_ok(cudaMalloc(&ctl, sizeof(Ctl)), "control block")) return -1;
         if (!cuda_ok(cudaMalloc(&red, sizeof(unsigned long long)), "reduction")) return -1;
+        if (!cuda_ok(cudaMalloc(&work, 3 * sizeof(unsigned int)), "work counters")) return -1;
         using TS = Variants<R>;
         variants = TS::all(form == HYDRO_FORM_FP32_LEARNED, rs);
         if (form == HYDRO_FORM_FP32_LEARNED) {
@@ -392,6 +410,12 @@ public:
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
                          "carveout attr"))
                 return -1;
+            if (v.strip) {
+                if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v.occ, v.kern, v.NT, v.smem),
+                             "occupancy"))
+                    return -1;
+                continue;  // (occ < 1: dropped below)
+            }
             if (v.tma) {
                 if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v.occ, v.kern, v.NT, v.smem),
                              "occupancy"))
@@ -410,7 +434,7 @@ public:
         {
             std::vector<StepVariant<R>> keep;
             for (auto& v : variants)
-                if (!v.tma || v.occ >= 1)
+                if ((!v.tma && !v.strip) || v.occ >= 1)
                     keep.push_back(v);
             variants.swap(keep);
         }
@@ -467,6 +491,7 @@ public:
         cudaFree(ctl);
         cudaFree(stage);
         cudaFree(red);
+        cudaFree(work);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -734,7 +759,7 @@ public:
         shape[1] = s.TI;
         shape[2] = s.NT;
         shape[3] = s.MINB;
-        shape[4] = s.tma;
+        shape[4] = s.strip ? 3 : s.tma;
     }
 
     // Times every variant on `steps` steps of the uploaded state (restored
@@ -792,6 +817,7 @@ public:
         double hs = cfl_hsmax(rc.gamma, fmin(rc.hx, rc.hy));
         RunPlan plan = plan_run(rc, hs, split, time_plot, N_plot, N_T);
         if (!cuda_ok(cudaMemsetAsync(ctl, 0, sizeof(Ctl), stream), "ctl clear")) return -1;
+        if (!cuda_ok(cudaMemsetAsync(work, 0, 3 * sizeof(unsigned int), stream), "work counters")) return -1;
 
         StepArgs<R> a;
         memset(&a, 0, sizeof(a));
@@ -870,7 +896,15 @@ public:
             if (r.dir == 0) {
                 a.src_s = Sx(s); a.dst_s = Sx(s ^ 1);
                 a.src_t = Ty(t); a.dst_t = Ty(t ^ 1);
-                if (V.tma) {
+                if (V.strip) {
+                    StripArgs sa;
+                    sa.work = work;
+                    sa.seg = V.TJ;
+                    void* args[] = {(void*)&a, (void*)&sa};
+                    if (!cuda_ok(cudaLaunchKernel(V.kern, dim3(sms * V.occ), dim3(V.NT), args, V.smem, stream),
+                                 "step launch"))
+                        return -1;
+                } else if (V.tma) {
                     // the boxes read the state buffer w, whose slope planes are s = t = w here
                     StepMaps mp = V.maps[w];
                     void* args[] = {(void*)&a, (void*)&mp};

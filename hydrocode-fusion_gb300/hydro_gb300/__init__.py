@@ -240,8 +240,9 @@ class Solver2D:
     def variant(self):
         shape = (ctypes.c_int * 5)()
         v = lib().hydro2d_get_variant(self._h, shape)
+        kind = {0: "tile", 1: "tma", 2: "tma", 3: "strip"}[int(shape[4])]
         return int(v), {"tile_x": shape[0], "tile_y": shape[1], "threads": shape[2], "min_ctas_per_sm": shape[3],
-                        "tma": bool(shape[4]), "tma_stages": int(shape[4])}
+                        "kernel": kind, "tma": kind == "tma", "tma_stages": int(shape[4]) if kind == "tma" else 0}
 
     def autotune(self, cfg, steps=3):
         """Time every kernel variant on `steps` steps of the uploaded state (restored

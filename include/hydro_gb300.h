@@ -146,7 +146,9 @@ int hydro1d_run_lag(int m, double *rho, double *u, double *p, double *E, double 
                     int order, hydro_run_info *info);
 /* Kernel variants of the unsplit step (tile shape / threads / occupancy).
  * hydro2d_get_variant fills shape[5] = {tile x, tile y, threads, min CTAs per SM,
- * shared-memory stages of the persistent TMA-staged kernel (1 or 2), 0 for one CTA per tile}. */
+ * kind}: kind 0 = one CTA per tile, 1 or 2 = the persistent TMA-staged kernel
+ * with that many shared-memory stages, 3 = the FP32 strip kernel (tile x = rows
+ * per work unit, tile y = columns a strip updates). */
 int hydro2d_num_variants(hydro2d_t *h);
 int hydro2d_set_variant(hydro2d_t *h, int v);
 int hydro2d_get_variant(hydro2d_t *h, int *shape);
