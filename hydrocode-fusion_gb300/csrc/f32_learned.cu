@@ -5,7 +5,7 @@ namespace hydro {
 
 void variants_f32_learned(std::vector<StepVariant<float>>& v)
 {
-    // the TMA-staged kernels first: index 0 is the default when nothing is tuned
+    // the TMA-staged kernels before the gathered ones
     v.push_back(tma_variant<float, 32, 32, 512, 1, true>());
     v.push_back(tma_variant<float, 32, 32, 384, 1, true>());
     v.push_back(tma_variant<float, 16, 32, 256, 2, true, 1>());

@@ -42,6 +42,7 @@ struct StepVariant {
     int occ = 0;
     StepMaps maps[2];  // tma: descriptors of the two state buffers
     int strip = 0;
+    int carve = 100;   // shared-memory carve-out of the L1/shared storage, per cent
 };
 
 template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int RS = 0>
@@ -60,11 +61,12 @@ StepVariant<R> tma_variant()
 }
 
 template <int NW, int MINB, bool LEARNED>
-StepVariant<float> strip_variant(int seg)
+StepVariant<float> strip_variant(int seg, int carve)
 {
     StepVariant<float> v{seg, STRIP_W, NW * 32, MINB, StripSmem<NW, LEARNED>::bytes,
                          (const void*)k_step_strip<NW, MINB, LEARNED>, 0, 0, {}};
     v.strip = 1;
+    v.carve = carve;
     return v;
 }
 
@@ -102,13 +104,13 @@ template <> struct Variants<float> {
         if (rs == HYDRO_SOLVER_G2D) {
             variants_f32_g2d(v);
         } else if (learned) {
-            variants_f32_learned(v);
+            // the strip kernels first: index 0 is the default when nothing is tuned
             variants_f32_strip(v, true);
+            variants_f32_learned(v);
         } else {
-            // the TMA-staged kernels first: index 0 is the default when nothing is tuned
+            variants_f32_strip(v, false);
             variants_f32_tma(v);
             variants_f32_gathered(v);
-            variants_f32_strip(v, false);
         }
         return v;
     }
@@ -406,8 +408,9 @@ public:
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem),
                          "smem attr"))
                 return -1;
-            // all of the unified L1/shared storage as shared memory, so several CTAs fit per SM
-            if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+            // the unified L1/shared storage: all of it as shared memory (several tile CTAs fit
+            // per SM), or part of it left as L1 (the strip kernel's register spills)
+            if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributePreferredSharedMemoryCarveout, v.carve),
                          "carveout attr"))
                 return -1;
             if (v.strip) {

@@ -36,6 +36,10 @@ namespace hydro {
 constexpr int STRIP_W = 60;      // columns a strip updates (64 loaded)
 constexpr int STRIP_QCAP = 64;   // queued faces per warp per flush
 constexpr int STRIP_QWORDS = 28; // words per queue entry
+// The learned form runs the network on a flush of at least this many faces:
+// one warp pass of the network costs about as much as the Newton iterations
+// it saves on a full warp of faces, so on a handful it would only add time.
+constexpr int STRIP_MLP_MIN = 16;
 
 // ---------------------------------------------------------------------------
 // packed FP32
@@ -74,28 +78,29 @@ struct SSide2 {
 // ---------------------------------------------------------------------------
 // limiter
 // ---------------------------------------------------------------------------
-// minmod3(alpha dL/h, alpha dR/h, sp) with ah = alpha/h: zero unless the three
-// share a sign, else the smallest magnitude with that sign
-__device__ __forceinline__ float strip_mm3(float dL, float dR, float sp, float ah)
+// minmod3(a, b, sp) of the scaled differences a = alpha dL/h, b = alpha dR/h:
+// zero unless the three share a sign, else the smallest magnitude with that sign
+__device__ __forceinline__ float strip_mm3(float a, float b, float sp)
 {
-    const float mag = fminf(fminf(fabsf(dL), fabsf(dR)) * ah, fabsf(sp));
-    const unsigned bL = __float_as_uint(dL), bR = __float_as_uint(dR), bM = __float_as_uint(sp);
-    const bool agree = (int)((bL ^ bM) | (bR ^ bM)) >= 0;
-    return agree ? __uint_as_float(__float_as_uint(mag) | (bM & 0x80000000u)) : 0.f;
+    const float mag = fminf(fminf(fabsf(a), fabsf(b)), fabsf(sp));
+    const unsigned ba = __float_as_uint(a), bb = __float_as_uint(b), bm = __float_as_uint(sp);
+    const bool agree = (int)((ba ^ bm) | (bb ^ bm)) >= 0;
+    return agree ? __uint_as_float(__float_as_uint(mag) | (bm & 0x80000000u)) : 0.f;
 }
-// minmod2(dL/h, dR/h) (the first limiting of a run) with ih = 1/h
-__device__ __forceinline__ float strip_mm2(float dL, float dR, float ih)
+// minmod2(a, b) of a = dL/h, b = dR/h (the first limiting of a run)
+__device__ __forceinline__ float strip_mm2(float a, float b)
 {
-    const float mag = fminf(fabsf(dL), fabsf(dR)) * ih;
-    const unsigned bL = __float_as_uint(dL), bR = __float_as_uint(dR);
-    return (int)(bL ^ bR) >= 0 ? __uint_as_float(__float_as_uint(mag) | (bL & 0x80000000u)) : 0.f;
+    const float mag = fminf(fabsf(a), fabsf(b));
+    const unsigned ba = __float_as_uint(a), bb = __float_as_uint(b);
+    return (int)(ba ^ bb) >= 0 ? __uint_as_float(__float_as_uint(mag) | (ba & 0x80000000u)) : 0.f;
 }
 __device__ __forceinline__ float2 strip_limit(float2 wl, float2 wc, float2 wr, float2 sp, bool find, float ah, float ih)
 {
-    const float2 dL = p_sub(wc, wl), dR = p_sub(wr, wc);
+    const float2 k = p_s(find ? ah : ih);
+    const float2 a = p_mul(p_sub(wc, wl), k), b = p_mul(p_sub(wr, wc), k);
     if (find)
-        return make_float2(strip_mm3(dL.x, dR.x, sp.x, ah), strip_mm3(dL.y, dR.y, sp.y, ah));
-    return make_float2(strip_mm2(dL.x, dR.x, ih), strip_mm2(dL.y, dR.y, ih));
+        return make_float2(strip_mm3(a.x, b.x, sp.x), strip_mm3(a.y, b.y, sp.y));
+    return make_float2(strip_mm2(a.x, b.x), strip_mm2(a.y, b.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -207,13 +212,13 @@ __device__ __forceinline__ void strip_ghost_cols(const StepArgs<float>& a, int c
 // the acoustic (uniform-pair) GRP case of a face pair, packed
 // (linear_grp_solver_Edir_Q1D.c:92-254 with lambda = 0), then GRP_2D_flux's
 // outputs (flux_solver.c:195-220).  Derivatives are carried negated (nD = -D).
-// uni: each element is a uniform pair.  code: 0, 1 (ifvar_check) or 2 (the
-// star/derivative check: the face must be redone in FP64); for elements that
-// are not uniform the outputs are meaningless (the queue replaces them).
+// uni: each element is a uniform pair.  code: 0, 1 (ifvar_check's positivity)
+// or 2 (the star/derivative check failed, or an output is not finite: the face
+// is redone in FP64, which decides its code); for elements that are not
+// uniform the outputs are meaningless (the queue replaces them).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void strip_face_pair(const SSide2& L, const SSide2& R, float2 slsum, const Gas<float>& G,
-                                                float tau, float htau, SF2& o, bool& uni_x, bool& uni_y, int& code_x,
-                                                int& code_y)
+__device__ __forceinline__ void strip_face_pair(const SSide2& L, const SSide2& R, const Gas<float>& G, float tau,
+                                                float htau, SF2& o, bool& uni_x, bool& uni_y, int& code_x, int& code_y)
 {
     const unsigned FULL = 0xffffffffu;
     // uniform-pair test (face_uniform<float>): squared distance against the
@@ -227,79 +232,58 @@ __device__ __forceinline__ void strip_face_pair(const SSide2& L, const SSide2& R
         uni_x = d2.x < thx * thx;
         uni_y = d2.y < thy * thy;
     }
-    // ifvar_check: positive pressure and density, finite slopes
-    const float2 mpr = make_float2(fminf(fminf(L.x[X_P].x, R.x[X_P].x), fminf(L.x[X_RHO].x, R.x[X_RHO].x)),
-                                   fminf(fminf(L.x[X_P].y, R.x[X_P].y), fminf(L.x[X_RHO].y, R.x[X_RHO].y)));
-    code_x = (mpr.x < G.eps || !(slsum.x <= 3.402823466e38f)) ? 1 : 0;
-    code_y = (mpr.y < G.eps || !(slsum.y <= 3.402823466e38f)) ? 1 : 0;
+    // ifvar_check's positivity of pressure and density on both sides
+    code_x = fminf(fminf(L.x[X_P].x, R.x[X_P].x), fminf(L.x[X_RHO].x, R.x[X_RHO].x)) < G.eps ? 1 : 0;
+    code_y = fminf(fminf(L.x[X_P].y, R.x[X_P].y), fminf(L.x[X_RHO].y, R.x[X_RHO].y)) < G.eps ? 1 : 0;
 
-    const float2 g2 = p_s(G.g);
-    const float2 irL = p_rcp(L.x[X_RHO]), irR = p_rcp(R.x[X_RHO]);
-    const float2 cL2 = p_mul(p_mul(g2, L.x[X_P]), irL), cR2 = p_mul(p_mul(g2, R.x[X_P]), irR);
-    const float2 cL = p_sqrt(cL2), cR = p_sqrt(cR2);
-    const float2 us = p_mul(p_s(0.5f), p_add(R.x[X_U], L.x[X_U]));
-    const float2 ps = p_mul(p_s(0.5f), p_add(R.x[X_P], L.x[X_P]));
-    const float2 spL = p_sub(us, cL), spR = p_add(us, cR);
-    // subsonic: the t-axis lies in the star region, upwind of the contact
-    const bool px = us.x > 0.f, py = us.y > 0.f;
-    float2 U0 = p_sel(px, py, L.x[X_RHO], R.x[X_RHO]);
-    float2 U1 = us;
-    float2 U2 = p_sel(px, py, L.x[X_V], R.x[X_V]);
-    float2 U3 = ps;
-    float2 C2 = p_sel(px, py, cL2, cR2);
-    float2 iU0 = p_sel(px, py, irL, irR);
-    const float2 C = p_sel(px, py, cL, cR);
-    const float2 rc = p_mul(U0, C);
-    const float2 irc = p_rcp(rc);
     const float2 h = p_s(0.5f);
+    const float2 irL = p_rcp(L.x[X_RHO]), irR = p_rcp(R.x[X_RHO]);
+    const float2 cL2 = p_mul(p_mul(p_s(G.g), L.x[X_P]), irL), cR2 = p_mul(p_mul(p_s(G.g), R.x[X_P]), irR);
+    const float2 rsL = make_float2(rsqrtf(cL2.x), rsqrtf(cL2.y)), rsR = make_float2(rsqrtf(cR2.x), rsqrtf(cR2.y));
+    const float2 cL = p_mul(cL2, rsL), cR = p_mul(cR2, rsR);
+    const float2 us = p_mul(h, p_add(R.x[X_U], L.x[X_U]));
+    const float2 ps = p_mul(h, p_add(R.x[X_P], L.x[X_P]));
+    const float2 spL = p_sub(us, cL), spR = p_add(us, cR);
+    // the side upwind of the contact (u* > 0: left); a supersonic t-axis
+    // (speed_L > 0 or speed_R < 0) lies on that side too
+    const bool px = us.x > 0.f, py = us.y > 0.f;
+    const float2 U0 = p_sel(px, py, L.x[X_RHO], R.x[X_RHO]);
+    const float2 U2 = p_sel(px, py, L.x[X_V], R.x[X_V]);
+    const float2 C2 = p_sel(px, py, cL2, cR2);
+    const float2 rsX = p_sel(px, py, rsL, rsR);
+    const float2 iU0 = p_sel(px, py, irL, irR);
+    const float2 Dv = p_sel(px, py, L.x[X_DV], R.x[X_DV]);
+    const float2 Tv = p_sel(px, py, L.x[X_TV], R.x[X_TV]);
+    const float2 dpX = p_sel(px, py, L.x[X_DP], R.x[X_DP]), tpX = p_sel(px, py, L.x[X_TP], R.x[X_TP]);
+    const float2 drX = p_sel(px, py, L.x[X_DRHO], R.x[X_DRHO]), trX = p_sel(px, py, L.x[X_TRHO], R.x[X_TRHO]);
+    // subsonic: the t-axis state is the star state (acoustic case)
+    const float2 rc = p_mul(U0, p_mul(C2, rsX));  // rho c
+    const float2 irc = p_mul(iU0, rsX);           // 1/(rho c)
+    const float2 icc = p_mul(rsX, rsX);           // 1/c^2
     float2 Dp = p_mul(h, p_sub(p_fma(L.x[X_DU], rc, L.x[X_DP]), p_fma(R.x[X_DU], rc, p_mul(p_s(-1.f), R.x[X_DP]))));
     float2 Tp = p_mul(h, p_sub(p_fma(L.x[X_TU], rc, L.x[X_TP]), p_fma(R.x[X_TU], rc, p_mul(p_s(-1.f), R.x[X_TP]))));
     float2 Du = p_mul(h, p_fma(p_sub(L.x[X_DP], R.x[X_DP]), irc, p_add(L.x[X_DU], R.x[X_DU])));
     float2 Tu = p_mul(h, p_fma(p_sub(L.x[X_TP], R.x[X_TP]), irc, p_add(L.x[X_TU], R.x[X_TU])));
-    const float2 icc = p_rcp(C2);
-    float2 Dv = p_sel(px, py, L.x[X_DV], R.x[X_DV]);
-    float2 Tv = p_sel(px, py, L.x[X_TV], R.x[X_TV]);
-    float2 Drho = p_fma(p_sub(Dp, p_sel(px, py, L.x[X_DP], R.x[X_DP])), icc, p_sel(px, py, L.x[X_DRHO], R.x[X_DRHO]));
-    float2 Trho = p_fma(p_sub(Tp, p_sel(px, py, L.x[X_TP], R.x[X_TP])), icc, p_sel(px, py, L.x[X_TRHO], R.x[X_TRHO]));
-    // supersonic: the t-axis sees one side's own state and derivatives
-    const bool slx = spL.x > 0.f, sly = spL.y > 0.f, srx = spR.x < 0.f, sry = spR.y < 0.f;
-    if (__any_sync(FULL, slx | sly | srx | sry)) {
-        const bool ax = slx | srx, ay = sly | sry;
-        auto pick = [&](float2& d, float2 l, float2 r) {
-            const float2 s = p_sel(slx, sly, l, r);
-            d = p_sel(ax, ay, s, d);
-        };
-        pick(U0, L.x[X_RHO], R.x[X_RHO]);
-        pick(U1, L.x[X_U], R.x[X_U]);
-        pick(U2, L.x[X_V], R.x[X_V]);
-        pick(U3, L.x[X_P], R.x[X_P]);
-        pick(C2, cL2, cR2);
-        pick(iU0, irL, irR);
-        pick(Drho, L.x[X_DRHO], R.x[X_DRHO]);
-        pick(Du, L.x[X_DU], R.x[X_DU]);
-        pick(Dv, L.x[X_DV], R.x[X_DV]);
-        pick(Dp, L.x[X_DP], R.x[X_DP]);
-        pick(Trho, L.x[X_TRHO], R.x[X_TRHO]);
-        pick(Tu, L.x[X_TU], R.x[X_TU]);
-        pick(Tv, L.x[X_TV], R.x[X_TV]);
-        pick(Tp, L.x[X_TP], R.x[X_TP]);
+    float2 Drho = p_fma(p_sub(Dp, dpX), icc, drX);
+    float2 Trho = p_fma(p_sub(Tp, tpX), icc, trX);
+    float2 U1 = us, U3 = ps;
+    const bool ax = spL.x > 0.f || spR.x < 0.f, ay = spL.y > 0.f || spR.y < 0.f;
+    if (__any_sync(FULL, ax | ay)) {
+        // supersonic: that side's own state and derivatives
+        U1 = p_sel(ax, ay, p_sel(px, py, L.x[X_U], R.x[X_U]), U1);
+        U3 = p_sel(ax, ay, p_sel(px, py, L.x[X_P], R.x[X_P]), U3);
+        Du = p_sel(ax, ay, p_sel(px, py, L.x[X_DU], R.x[X_DU]), Du);
+        Tu = p_sel(ax, ay, p_sel(px, py, L.x[X_TU], R.x[X_TU]), Tu);
+        Dp = p_sel(ax, ay, dpX, Dp);
+        Tp = p_sel(ax, ay, tpX, Tp);
+        Drho = p_sel(ax, ay, drX, Drho);
+        Trho = p_sel(ax, ay, trX, Trho);
     }
     const float2 dvs = p_add(Du, Tv);
     const float2 nD0 = p_fma(U1, Drho, p_fma(U2, Trho, p_mul(U0, dvs)));
     const float2 nD1 = p_fma(U1, Du, p_fma(U2, Tu, p_mul(Dp, iU0)));
     const float2 nD2 = p_fma(U1, Dv, p_fma(U2, Tv, p_mul(Tp, iU0)));
     const float2 nD3 = p_fma(U1, Dp, p_fma(U2, Tp, p_mul(p_mul(U0, C2), dvs)));
-    // star_dire_check: positive t-axis density and pressure, finite values and derivatives
-    {
-        const float ux = fabsf(U0.x) + fabsf(U1.x) + fabsf(U2.x) + fabsf(U3.x) + fabsf(nD0.x) + fabsf(nD1.x) +
-                         fabsf(nD2.x) + fabsf(nD3.x);
-        const float uy = fabsf(U0.y) + fabsf(U1.y) + fabsf(U2.y) + fabsf(U3.y) + fabsf(nD0.y) + fabsf(nD1.y) +
-                         fabsf(nD2.y) + fabsf(nD3.y);
-        if (fminf(U0.x, U3.x) < G.eps || !(ux <= 3.402823466e38f))
-            code_x = 2;
-        if (fminf(U0.y, U3.y) < G.eps || !(uy <= 3.402823466e38f))
-            code_y = 2;
-    }
     // fluxes at t + tau/2 and values at t + tau
     const float2 mh = p_s(-htau), mt = p_s(-tau);
     const float2 rm = p_fma(mh, nD0, U0), am = p_fma(mh, nD1, U1), bm = p_fma(mh, nD2, U2), pm = p_fma(mh, nD3, U3);
@@ -313,6 +297,15 @@ __device__ __forceinline__ void strip_face_pair(const SSide2& L, const SSide2& R
     o.I[1] = p_fma(mt, nD1, U1);
     o.I[2] = p_fma(mt, nD2, U2);
     o.I[3] = p_fma(mt, nD3, U3);
+    // star_dire_check: positive t-axis density and pressure; a non-finite value
+    // or derivative shows in the outputs (s - s is 0 exactly when s is finite)
+    const float2 s = p_add(p_add(p_add(o.F[0], o.F[1]), p_add(o.F[2], o.F[3])),
+                           p_add(p_add(o.I[0], o.I[1]), p_add(o.I[2], o.I[3])));
+    const float2 z = p_sub(s, s);
+    if (fminf(U0.x, U3.x) < G.eps || !(z.x == 0.f))
+        code_x = 2;
+    if (fminf(U0.y, U3.y) < G.eps || !(z.y == 0.f))
+        code_y = 2;
 }
 
 // ---------------------------------------------------------------------------
@@ -352,8 +345,10 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StepArg
         const int row = __float_as_int(e[24]), col = __float_as_int(e[25]), fl = __float_as_int(e[26]);
         const bool ydir = fl & 1, retry = (fl >> 1) & 1, counted = (fl >> 2) & 1;
         float p_start = -1.f;
-        if constexpr (LEARNED)
-            p_start = learned_guess(L, Rr, act && !retry, a.G, *M, cnt - base < 32 ? cnt - base : 32);
+        if constexpr (LEARNED) {
+            if (cnt - base >= STRIP_MLP_MIN)  // warp-uniform
+                p_start = learned_guess(L, Rr, act && !retry, a.G, *M, cnt - base < 32 ? cnt - base : 32);
+        }
         if (!act)
             continue;
         FaceOut<float> o;
@@ -442,17 +437,6 @@ __device__ __forceinline__ void strip_queue(float* q, const SSide2& L, const SSi
         }
     }
     __syncwarp();
-}
-
-// Sum of the magnitudes of a cell pair's 8 slopes (ifvar_check's finiteness test)
-__device__ __forceinline__ float2 strip_slsum(const SS2& S)
-{
-    float2 r;
-    r.x = fabsf(S.s[0].x) + fabsf(S.s[1].x) + fabsf(S.s[2].x) + fabsf(S.s[3].x) + fabsf(S.t[0].x) + fabsf(S.t[1].x) +
-          fabsf(S.t[2].x) + fabsf(S.t[3].x);
-    r.y = fabsf(S.s[0].y) + fabsf(S.s[1].y) + fabsf(S.s[2].y) + fabsf(S.s[3].y) + fabsf(S.t[0].y) + fabsf(S.t[1].y) +
-          fabsf(S.t[2].y) + fabsf(S.t[3].y);
-    return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -563,7 +547,6 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
                 if (edge_cols)
                     strip_ghost_cols(a, c, S0);
             }
-            const float2 sum0 = strip_slsum(S0), summ = strip_slsum(Sm);
             // x-faces of row r: between cells (r-1, col) and (r, col)
             SF2 XF0;
             {
@@ -579,7 +562,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
                 }
                 bool ux, uy;
                 int kx, ky;
-                strip_face_pair(L, R, p_add(summ, sum0), G, a.tau, a.htau, XF0, ux, uy, kx, ky);
+                strip_face_pair(L, R, G, a.tau, a.htau, XF0, ux, uy, kx, ky);
                 const bool vx = upd_x, vy = upd_y;  // x-faces of the columns this strip updates
                 const bool qx = vx && (!ux || kx == 2), qy = vy && (!uy || ky == 2);
                 if (vx && !qx && kx)
@@ -625,7 +608,6 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
                         tl[k] = __shfl_up_sync(FULL, Sm.t[k].y, 1);
                         sl[k] = __shfl_up_sync(FULL, Sm.s[k].y, 1);
                     }
-                    const float sumL = __shfl_up_sync(FULL, summ.y, 1);
                     // normal frame of a y-face: normal velocity v, tangential -u; normal derivatives
                     // the y-slopes (t0, t2, -t1, t3), tangential the x-slopes (-s0, -s2, s1, -s3)
                     SSide2 L, R;
@@ -654,10 +636,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
                     R.x[X_TU] = p_mul(neg, Sm.s[2]);
                     R.x[X_TV] = Sm.s[1];
                     R.x[X_TP] = p_mul(neg, Sm.s[3]);
-                    const float2 ss = make_float2(sumL + summ.x, summ.x + summ.y);
                     bool ux, uy;
                     int kx, ky;
-                    strip_face_pair(L, R, ss, G, a.tau, a.htau, YF, ux, uy, kx, ky);
+                    strip_face_pair(L, R, G, a.tau, a.htau, YF, ux, uy, kx, ky);
                     const bool qx = needA && (!ux || kx == 2), qy = needB && (!uy || ky == 2);
                     if (needA && !qx && kx)
                         report_face(a.ctl, slot, 1, (unsigned long long)q1 * (n + 1) + cA, kx);
