@@ -78,11 +78,13 @@ __device__ __forceinline__ bool grid_barrier(const BatchDev& B)
             atomicAdd(B.bar_gen, 1u);
         } else {
             const unsigned long long t0 = global_ns();
+            // the timer is read every 1024 polls, every poll under a limit of 100 us
+            const unsigned int mask = B.wait_ns < 100000ull ? 0u : 1023u;
             unsigned int polls = 0;
             while (*gen == g) {
                 __nanosleep(100);
                 // the poll count also ends the wait should the timer not advance
-                if ((++polls & 1023u) == 0u && (global_ns() - t0 > B.wait_ns || polls > (1u << 30))) {
+                if ((++polls & mask) == 0u && (global_ns() - t0 > B.wait_ns || polls > (1u << 30))) {
                     atomicExch(B.bar_err, 1);
                     break;
                 }

@@ -230,3 +230,39 @@ def test_batch_sizes_are_seeded_and_in_range():
     Ns = {m for m, n in s1}
     assert all(m == n for m, n in s1)
     assert Ns <= set(range(64, 513, 32)) and len(Ns) == 15
+
+
+@pytest.mark.gpu
+def test_batch_barrier_wait_runs_out(gpu_lib):
+    """The persistent schedule's grid barrier gives up when its wait limit runs
+    out: with a limit of a nanosecond the first block to arrive stops waiting,
+    every block leaves the time loop, the run returns -2 with the barrier error
+    reported, and the same handle then runs normally with the limit restored."""
+    hg = gpu_lib
+    probs = _problems(hg)
+    cfg = _cfg(hg)
+    b = hg.Batch(SIZES)
+    try:
+        b.set_schedule(0, 0)  # one persistent cooperative kernel for all steps
+        for k, (rho, u, v, p) in enumerate(probs):
+            b.upload(k, rho, u, v, p, gamma=float(cfg[6]))
+        b.set_wait_limit(1e-9)
+        info = hg.BatchInfo()
+        c = np.ascontiguousarray(cfg, np.float64)
+        L = hg.lib()
+        L.hydro_batch_run.restype = ctypes.c_int
+        rc = L.hydro_batch_run(b._h, c, len(c), STEPS, 0, ctypes.byref(info))
+        assert rc == -2, rc
+        assert "barrier" in hg.last_error()
+        b.set_wait_limit(5.0)
+        for k, (rho, u, v, p) in enumerate(probs):
+            b.upload(k, rho, u, v, p, gamma=float(cfg[6]))
+        info = b.run(cfg, STEPS)
+        assert info.steps == STEPS and info.halted_problems == 0
+        got = [b.download(k) for k in range(len(SIZES))]
+    finally:
+        b.close()
+    ref, _, _ = _run_batch(hg, probs, cfg, 0, 0)
+    for k in range(len(SIZES)):
+        for f in FIELDS:
+            assert np.array_equal(got[k][f], ref[k][f])
