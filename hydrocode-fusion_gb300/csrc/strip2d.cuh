@@ -454,6 +454,270 @@ struct StripSmem {
     static constexpr size_t bytes = mlp_off + (LEARNED ? sizeof(MlpShared) : 0);
 };
 
+// One work unit of a step: columns [c0, c0 + STRIP_W) of rows [r0, r1) of the
+// grid a describes, marched by the calling warp (warp-collective).  The
+// update's positivity flag and the Newton statistics accumulate in the
+// caller's bad and stats3 (see strip_report).
+template <bool LEARNED>
+__device__ __forceinline__ void strip_unit(const StepArgs<float>& a, int c0, int r0, int r1, float* q,
+                                           const MlpShared* M, int* stats3, unsigned& bad)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int m = a.m, n = a.n, slot = a.seq % 3;
+    const Gas<float>& G = a.G;
+    const float ihx = a.pow2_x ? a.inv_hx : 1.f / a.hx, ihy = a.pow2_y ? a.inv_hy : 1.f / a.hy;
+    const float ahx = a.alpha * ihx, ahy = a.alpha * ihy;
+    const float hhx = a.hhx, hhy = a.hhy;
+    const bool ghost_rows = a.bx != -7, ghost_cols = a.by != -7;
+    const int c = c0 - 2 + 2 * lane;
+    const bool colfast = c >= 0 && c + 1 < n;
+    const bool edge_cols = ghost_cols && !__all_sync(FULL, colfast);
+    // columns this lane's cells update / faces it owns
+    const bool upd_x = lane >= 1 && lane <= 30 && c < n, upd_y = lane >= 1 && lane <= 30 && c + 1 < n;
+    // y-faces: A at column c (between c-1 and c), B at c+1 (between c and c+1); needed for columns in
+    // [c0, min(c0+60, n)]; the statistics count each face once (face n with the last strip)
+    const int cA = c, cB = c + 1;
+    const bool needA = lane >= 1 && cA >= c0 && cA <= c0 + STRIP_W && cA <= n;
+    const bool needB = lane >= 1 && cB >= c0 && cB <= c0 + STRIP_W && cB <= n;
+    const bool ownA = needA && (cA < c0 + STRIP_W || cA == n), ownB = needB && (cB < c0 + STRIP_W || cB == n);
+
+    // prologue: values of rows r0-2 .. r0+1, previous slopes of rows r0-1, r0
+    SV2 Vm, V0, Vp, Va;
+    SS2 Sm, P;
+    {
+        auto rowfast = [&](int j) { return colfast && j >= 0 && j < m; };
+        strip_load_vals(a, r0 - 2, c, rowfast(r0 - 2), Va);
+        strip_load_vals(a, r0 - 1, c, rowfast(r0 - 1), Vm);
+        strip_load_vals(a, r0, c, rowfast(r0), V0);
+        strip_load_vals(a, r0 + 1, c, rowfast(r0 + 1), Vp);
+        SS2 Pm;
+        strip_load_prev(a, r0 - 1, c, rowfast(r0 - 1), Pm);
+        strip_load_prev(a, r0, c, rowfast(r0), P);
+        if (r0 == 0 && ghost_rows) {
+            // slopes of ghost row -1 from row 0's
+            SS2 S0;
+            strip_slopes(a, Vm, V0, Vp, P, ahx, ihx, ahy, ihy, S0);
+            if (edge_cols)
+                strip_ghost_cols(a, c, S0);
+            strip_ghost_row(a, S0, true, Sm);
+        } else {
+            strip_slopes(a, Va, Vm, V0, Pm, ahx, ihx, ahy, ihy, Sm);
+            if (edge_cols)
+                strip_ghost_cols(a, c, Sm);
+        }
+    }
+    float2 E = make_float2(0.f, 0.f);
+    SF2 XFm;
+#pragma unroll 1
+    for (int r = r0; r <= r1; ++r) {
+        // slopes of row r
+        SS2 S0;
+        if (r == m && ghost_rows) {
+            strip_ghost_row(a, Sm, false, S0);
+        } else {
+            strip_slopes(a, Vm, V0, Vp, P, ahx, ihx, ahy, ihy, S0);
+            if (edge_cols)
+                strip_ghost_cols(a, c, S0);
+        }
+        // x-faces of row r: between cells (r-1, col) and (r, col)
+        SF2 XF0;
+        {
+            SSide2 L, R;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                L.x[X_RHO + k] = p_fma(p_s(hhx), Sm.s[k], Vm.w[k]);
+                L.x[X_DRHO + k] = Sm.s[k];
+                L.x[X_TRHO + k] = Sm.t[k];
+                R.x[X_RHO + k] = p_fma(p_s(-hhx), S0.s[k], V0.w[k]);
+                R.x[X_DRHO + k] = S0.s[k];
+                R.x[X_TRHO + k] = S0.t[k];
+            }
+            bool ux, uy;
+            int kx, ky;
+            strip_face_pair(L, R, G, a.tau, a.htau, XF0, ux, uy, kx, ky);
+            const bool vx = upd_x, vy = upd_y;  // x-faces of the columns this strip updates
+            const bool qx = vx && (!ux || kx == 2), qy = vy && (!uy || ky == 2);
+            if (vx && !qx && kx)
+                report_face(a.ctl, slot, 0, (unsigned long long)c * (m + 1) + r, kx);
+            if (vy && !qy && ky)
+                report_face(a.ctl, slot, 0, (unsigned long long)(c + 1) * (m + 1) + r, ky);
+            const bool own_row = r < r1 || r == m;
+            strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, own_row, own_row, false, r, c, r, c + 1, a, M,
+                                 stats3, XF0);
+        }
+        // prefetch the next rows (after the x-faces, while the y-faces are computed)
+        SV2 Vn;
+        SS2 Pn;
+        float2 En = make_float2(0.f, 0.f);
+        if (r < r1) {
+            const bool fv = colfast && r + 2 < m && r + 2 >= 0;
+            strip_load_vals(a, r + 2, c, fv, Vn);
+            strip_load_prev(a, r + 1, c, colfast && r + 1 < m, Pn);
+            if (colfast)
+                En = ldg2(a.src_w + 4 * a.plane + (size_t)r * a.ld + c);
+            else if (upd_x || upd_y) {
+                const size_t o = (size_t)r * a.ld;
+                En = make_float2(upd_x ? a.src_w[4 * a.plane + o + c] : 0.f,
+                                 upd_y ? a.src_w[4 * a.plane + o + c + 1] : 0.f);
+            }
+        }
+        if (r > r0) {
+            // y-faces of row r-1 (Vm, Sm): A between columns c-1 and c, B between c and c+1
+            const int q1 = r - 1;
+            SF2 YF;
+            {
+                float2 plus[4], minus[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    plus[k] = p_fma(p_s(hhy), Sm.t[k], Vm.w[k]);
+                    minus[k] = p_fma(p_s(-hhy), Sm.t[k], Vm.w[k]);
+                }
+                // column c-1 (the lane below's second column)
+                float pl[4], tl[4], sl[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    pl[k] = __shfl_up_sync(FULL, plus[k].y, 1);
+                    tl[k] = __shfl_up_sync(FULL, Sm.t[k].y, 1);
+                    sl[k] = __shfl_up_sync(FULL, Sm.s[k].y, 1);
+                }
+                // normal frame of a y-face: normal velocity v, tangential -u; normal derivatives
+                // the y-slopes (t0, t2, -t1, t3), tangential the x-slopes (-s0, -s2, s1, -s3)
+                SSide2 L, R;
+                L.x[X_RHO] = make_float2(pl[0], plus[0].x);
+                L.x[X_U] = make_float2(pl[2], plus[2].x);
+                L.x[X_V] = make_float2(-pl[1], -plus[1].x);
+                L.x[X_P] = make_float2(pl[3], plus[3].x);
+                L.x[X_DRHO] = make_float2(tl[0], Sm.t[0].x);
+                L.x[X_DU] = make_float2(tl[2], Sm.t[2].x);
+                L.x[X_DV] = make_float2(-tl[1], -Sm.t[1].x);
+                L.x[X_DP] = make_float2(tl[3], Sm.t[3].x);
+                L.x[X_TRHO] = make_float2(-sl[0], -Sm.s[0].x);
+                L.x[X_TU] = make_float2(-sl[2], -Sm.s[2].x);
+                L.x[X_TV] = make_float2(sl[1], Sm.s[1].x);
+                L.x[X_TP] = make_float2(-sl[3], -Sm.s[3].x);
+                const float2 neg = p_s(-1.f);
+                R.x[X_RHO] = minus[0];
+                R.x[X_U] = minus[2];
+                R.x[X_V] = p_mul(neg, minus[1]);
+                R.x[X_P] = minus[3];
+                R.x[X_DRHO] = Sm.t[0];
+                R.x[X_DU] = Sm.t[2];
+                R.x[X_DV] = p_mul(neg, Sm.t[1]);
+                R.x[X_DP] = Sm.t[3];
+                R.x[X_TRHO] = p_mul(neg, Sm.s[0]);
+                R.x[X_TU] = p_mul(neg, Sm.s[2]);
+                R.x[X_TV] = Sm.s[1];
+                R.x[X_TP] = p_mul(neg, Sm.s[3]);
+                bool ux, uy;
+                int kx, ky;
+                strip_face_pair(L, R, G, a.tau, a.htau, YF, ux, uy, kx, ky);
+                const bool qx = needA && (!ux || kx == 2), qy = needB && (!uy || ky == 2);
+                if (needA && !qx && kx)
+                    report_face(a.ctl, slot, 1, (unsigned long long)q1 * (n + 1) + cA, kx);
+                if (needB && !qy && ky)
+                    report_face(a.ctl, slot, 1, (unsigned long long)q1 * (n + 1) + cB, ky);
+                strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, ownA, ownB, true, q1, cA, q1, cB, a,
+                                     M, stats3, YF);
+            }
+            // update of row r-1: x-faces r-1 (XFm) and r (XF0), y-faces A, B and the next lane's A
+            float2 Ar[8];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                Ar[t] = make_float2(YF.F[t].y, __shfl_down_sync(FULL, YF.F[t].x, 1));
+                Ar[4 + t] = make_float2(YF.I[t].y, __shfl_down_sync(FULL, YF.I[t].x, 1));
+            }
+            if (upd_x || upd_y) {
+                const float2 nu = p_s(a.nu), mu = p_s(a.mu);
+                // y-face fluxes in the global frame: x-momentum -Ft, y-momentum Fn
+                const float2 dFx0 = p_sub(XF0.F[0], XFm.F[0]), dFy0 = p_sub(Ar[0], YF.F[0]);
+                const float2 dFx1 = p_sub(XF0.F[1], XFm.F[1]), dFy1 = p_sub(YF.F[2], Ar[2]);  // -(Ft_r - Ft_l)
+                const float2 dFx2 = p_sub(XF0.F[2], XFm.F[2]), dFy2 = p_sub(Ar[1], YF.F[1]);
+                const float2 dFx3 = p_sub(XF0.F[3], XFm.F[3]), dFy3 = p_sub(Ar[3], YF.F[3]);
+                const float2 rho = Vm.w[0];
+                const float2 mom_x = p_sub(p_sub(p_mul(rho, Vm.w[1]), p_mul(nu, dFx1)), p_mul(mu, dFy1));
+                const float2 mom_y = p_sub(p_sub(p_mul(rho, Vm.w[2]), p_mul(nu, dFx2)), p_mul(mu, dFy2));
+                const float2 ene = p_sub(p_sub(p_mul(rho, E), p_mul(nu, dFx3)), p_mul(mu, dFy3));
+                const float2 rn = p_sub(p_sub(rho, p_mul(nu, dFx0)), p_mul(mu, dFy0));
+                const float2 irn = p_rcp(rn);
+                const float2 un = p_mul(mom_x, irn), vn = p_mul(mom_y, irn), En2 = p_mul(ene, irn);
+                const float2 pn = p_mul(p_sub(p_sub(ene, p_mul(p_mul(p_s(0.5f), mom_x), un)), p_mul(p_mul(p_s(0.5f), mom_y), vn)),
+                                        p_s(G.gm1));
+                if ((upd_x && (pn.x < G.eps || rn.x < G.eps)) || (upd_y && (pn.y < G.eps || rn.y < G.eps)))
+                    bad = 1u;
+                float2 ns[4], nt[4];
+                const float2 ihx2 = p_s(ihx), ihy2 = p_s(ihy);
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    ns[t] = p_mul(p_sub(XF0.I[t], XFm.I[t]), ihx2);
+                // y-face I in the global frame: (I0, -B, A, I3)
+                nt[0] = p_mul(p_sub(Ar[4], YF.I[0]), ihy2);
+                nt[1] = p_mul(p_sub(YF.I[2], Ar[6]), ihy2);
+                nt[2] = p_mul(p_sub(Ar[5], YF.I[1]), ihy2);
+                nt[3] = p_mul(p_sub(Ar[7], YF.I[3]), ihy2);
+                const size_t o = (size_t)q1 * a.ld + c;
+                float* dw = a.dst_w + o;
+                if (upd_x && upd_y) {
+                    *reinterpret_cast<float2*>(dw) = rn;
+                    *reinterpret_cast<float2*>(dw + a.plane) = un;
+                    *reinterpret_cast<float2*>(dw + 2 * a.plane) = vn;
+                    *reinterpret_cast<float2*>(dw + 3 * a.plane) = pn;
+                    *reinterpret_cast<float2*>(dw + 4 * a.plane) = En2;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        *reinterpret_cast<float2*>(a.dst_s + t * a.plane + o) = ns[t];
+                        *reinterpret_cast<float2*>(a.dst_t + t * a.plane + o) = nt[t];
+                    }
+                } else {  // upd_x only (the last column of the domain is this pair's first)
+                    dw[0] = rn.x;
+                    dw[a.plane] = un.x;
+                    dw[2 * a.plane] = vn.x;
+                    dw[3 * a.plane] = pn.x;
+                    dw[4 * a.plane] = En2.x;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        a.dst_s[t * a.plane + o] = ns[t].x;
+                        a.dst_t[t * a.plane + o] = nt[t].x;
+                    }
+                }
+            }
+        }
+        // advance
+        Vm = V0;
+        V0 = Vp;
+        Vp = Vn;
+        Sm = S0;
+        P = Pn;
+        XFm = XF0;
+        E = En;
+    }
+}
+
+// The warp's update positivity flag and Newton statistics into the control
+// block ctl (launch slot `slot`); clears them.  Warp-collective.
+__device__ __forceinline__ void strip_report(Ctl* ctl, int slot, int stats, int* stats3, unsigned& bad)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    if (__any_sync(FULL, bad != 0u) && lane == 0)
+        atomicOr(&ctl->upd_bad[slot], 1u);
+    if (stats) {
+        for (int off = 16; off; off >>= 1) {
+            stats3[0] += __shfl_xor_sync(FULL, stats3[0], off);
+            stats3[1] += __shfl_xor_sync(FULL, stats3[1], off);
+            stats3[2] += __shfl_xor_sync(FULL, stats3[2], off);
+        }
+        if (lane == 0 && stats3[0]) {
+            atomicAdd(&ctl->newton_faces, (unsigned long long)stats3[0]);
+            atomicAdd(&ctl->newton_iters, (unsigned long long)stats3[1]);
+            if (stats3[2])
+                atomicAdd(&ctl->newton_fallbacks, (unsigned long long)stats3[2]);
+        }
+    }
+    bad = 0u;
+    stats3[0] = stats3[1] = stats3[2] = 0;
+}
+
 template <int NW, int MINB, bool LEARNED>
 __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_constant__ StepArgs<float> a,
                                                               const __grid_constant__ StripArgs sa)
@@ -474,19 +738,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
     if (threadIdx.x == 0 && blockIdx.x == 0)
         sa.work[(a.seq + 1) % 3] = 0u;  // the next launch's counter (this launch's was cleared by the previous one)
     unsigned int* counter = sa.work + a.seq % 3;
-
-    const int m = a.m, n = a.n, slot = a.seq % 3;
-    const Gas<float>& G = a.G;
-    const int nstrip = (n + STRIP_W - 1) / STRIP_W;
-    const int nseg = (m + sa.seg - 1) / sa.seg;
-    const int nunits = nstrip * nseg;
-    const float ihx = a.pow2_x ? a.inv_hx : 1.f / a.hx, ihy = a.pow2_y ? a.inv_hy : 1.f / a.hy;
-    const float ahx = a.alpha * ihx, ahy = a.alpha * ihy;
-    const float hhx = a.hhx, hhy = a.hhy;
-    const bool ghost_rows = a.bx != -7, ghost_cols = a.by != -7;
+    const int nstrip = (a.n + STRIP_W - 1) / STRIP_W;
+    const int nunits = nstrip * ((a.m + sa.seg - 1) / sa.seg);
     int stats3[3] = {0, 0, 0};
     unsigned bad = 0;
-
     for (;;) {
         int u = 0;
         if (lane == 0)
@@ -495,245 +750,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
         if (u >= nunits)
             break;
         const int seg = u / nstrip, strip = u - seg * nstrip;
-        const int c0 = strip * STRIP_W, r0 = seg * sa.seg;
-        const int r1 = (r0 + sa.seg < m) ? r0 + sa.seg : m;
-        const int c = c0 - 2 + 2 * lane;
-        const bool colfast = c >= 0 && c + 1 < n;
-        const bool edge_cols = ghost_cols && !__all_sync(FULL, colfast);
-        // columns this lane's cells update / faces it owns
-        const bool upd_x = lane >= 1 && lane <= 30 && c < n, upd_y = lane >= 1 && lane <= 30 && c + 1 < n;
-        // y-faces: A at column c (between c-1 and c), B at c+1 (between c and c+1); needed for columns in
-        // [c0, min(c0+60, n)]; the statistics count each face once (face n with the last strip)
-        const int cA = c, cB = c + 1;
-        const bool needA = lane >= 1 && cA >= c0 && cA <= c0 + STRIP_W && cA <= n;
-        const bool needB = lane >= 1 && cB >= c0 && cB <= c0 + STRIP_W && cB <= n;
-        const bool ownA = needA && (cA < c0 + STRIP_W || cA == n), ownB = needB && (cB < c0 + STRIP_W || cB == n);
-
-        // prologue: values of rows r0-2 .. r0+1, previous slopes of rows r0-1, r0
-        SV2 Vm, V0, Vp, Va;
-        SS2 Sm, P;
-        {
-            auto rowfast = [&](int j) { return colfast && j >= 0 && j < m; };
-            strip_load_vals(a, r0 - 2, c, rowfast(r0 - 2), Va);
-            strip_load_vals(a, r0 - 1, c, rowfast(r0 - 1), Vm);
-            strip_load_vals(a, r0, c, rowfast(r0), V0);
-            strip_load_vals(a, r0 + 1, c, rowfast(r0 + 1), Vp);
-            SS2 Pm;
-            strip_load_prev(a, r0 - 1, c, rowfast(r0 - 1), Pm);
-            strip_load_prev(a, r0, c, rowfast(r0), P);
-            if (r0 == 0 && ghost_rows) {
-                // slopes of ghost row -1 from row 0's
-                SS2 S0;
-                strip_slopes(a, Vm, V0, Vp, P, ahx, ihx, ahy, ihy, S0);
-                if (edge_cols)
-                    strip_ghost_cols(a, c, S0);
-                strip_ghost_row(a, S0, true, Sm);
-            } else {
-                strip_slopes(a, Va, Vm, V0, Pm, ahx, ihx, ahy, ihy, Sm);
-                if (edge_cols)
-                    strip_ghost_cols(a, c, Sm);
-            }
-        }
-        float2 E = make_float2(0.f, 0.f);
-        SF2 XFm;
-#pragma unroll 1
-        for (int r = r0; r <= r1; ++r) {
-            // slopes of row r
-            SS2 S0;
-            if (r == m && ghost_rows) {
-                strip_ghost_row(a, Sm, false, S0);
-            } else {
-                strip_slopes(a, Vm, V0, Vp, P, ahx, ihx, ahy, ihy, S0);
-                if (edge_cols)
-                    strip_ghost_cols(a, c, S0);
-            }
-            // x-faces of row r: between cells (r-1, col) and (r, col)
-            SF2 XF0;
-            {
-                SSide2 L, R;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    L.x[X_RHO + k] = p_fma(p_s(hhx), Sm.s[k], Vm.w[k]);
-                    L.x[X_DRHO + k] = Sm.s[k];
-                    L.x[X_TRHO + k] = Sm.t[k];
-                    R.x[X_RHO + k] = p_fma(p_s(-hhx), S0.s[k], V0.w[k]);
-                    R.x[X_DRHO + k] = S0.s[k];
-                    R.x[X_TRHO + k] = S0.t[k];
-                }
-                bool ux, uy;
-                int kx, ky;
-                strip_face_pair(L, R, G, a.tau, a.htau, XF0, ux, uy, kx, ky);
-                const bool vx = upd_x, vy = upd_y;  // x-faces of the columns this strip updates
-                const bool qx = vx && (!ux || kx == 2), qy = vy && (!uy || ky == 2);
-                if (vx && !qx && kx)
-                    report_face(a.ctl, slot, 0, (unsigned long long)c * (m + 1) + r, kx);
-                if (vy && !qy && ky)
-                    report_face(a.ctl, slot, 0, (unsigned long long)(c + 1) * (m + 1) + r, ky);
-                const bool own_row = r < r1 || r == m;
-                strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, own_row, own_row, false, r, c, r, c + 1, a, M,
-                                     stats3, XF0);
-            }
-            // prefetch the next rows (after the x-faces, while the y-faces are computed)
-            SV2 Vn;
-            SS2 Pn;
-            float2 En = make_float2(0.f, 0.f);
-            if (r < r1) {
-                const bool fv = colfast && r + 2 < m && r + 2 >= 0;
-                strip_load_vals(a, r + 2, c, fv, Vn);
-                strip_load_prev(a, r + 1, c, colfast && r + 1 < m, Pn);
-                if (colfast)
-                    En = ldg2(a.src_w + 4 * a.plane + (size_t)r * a.ld + c);
-                else if (upd_x || upd_y) {
-                    const size_t o = (size_t)r * a.ld;
-                    En = make_float2(upd_x ? a.src_w[4 * a.plane + o + c] : 0.f,
-                                     upd_y ? a.src_w[4 * a.plane + o + c + 1] : 0.f);
-                }
-            }
-            if (r > r0) {
-                // y-faces of row r-1 (Vm, Sm): A between columns c-1 and c, B between c and c+1
-                const int q1 = r - 1;
-                SF2 YF;
-                {
-                    float2 plus[4], minus[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        plus[k] = p_fma(p_s(hhy), Sm.t[k], Vm.w[k]);
-                        minus[k] = p_fma(p_s(-hhy), Sm.t[k], Vm.w[k]);
-                    }
-                    // column c-1 (the lane below's second column)
-                    float pl[4], tl[4], sl[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        pl[k] = __shfl_up_sync(FULL, plus[k].y, 1);
-                        tl[k] = __shfl_up_sync(FULL, Sm.t[k].y, 1);
-                        sl[k] = __shfl_up_sync(FULL, Sm.s[k].y, 1);
-                    }
-                    // normal frame of a y-face: normal velocity v, tangential -u; normal derivatives
-                    // the y-slopes (t0, t2, -t1, t3), tangential the x-slopes (-s0, -s2, s1, -s3)
-                    SSide2 L, R;
-                    L.x[X_RHO] = make_float2(pl[0], plus[0].x);
-                    L.x[X_U] = make_float2(pl[2], plus[2].x);
-                    L.x[X_V] = make_float2(-pl[1], -plus[1].x);
-                    L.x[X_P] = make_float2(pl[3], plus[3].x);
-                    L.x[X_DRHO] = make_float2(tl[0], Sm.t[0].x);
-                    L.x[X_DU] = make_float2(tl[2], Sm.t[2].x);
-                    L.x[X_DV] = make_float2(-tl[1], -Sm.t[1].x);
-                    L.x[X_DP] = make_float2(tl[3], Sm.t[3].x);
-                    L.x[X_TRHO] = make_float2(-sl[0], -Sm.s[0].x);
-                    L.x[X_TU] = make_float2(-sl[2], -Sm.s[2].x);
-                    L.x[X_TV] = make_float2(sl[1], Sm.s[1].x);
-                    L.x[X_TP] = make_float2(-sl[3], -Sm.s[3].x);
-                    const float2 neg = p_s(-1.f);
-                    R.x[X_RHO] = minus[0];
-                    R.x[X_U] = minus[2];
-                    R.x[X_V] = p_mul(neg, minus[1]);
-                    R.x[X_P] = minus[3];
-                    R.x[X_DRHO] = Sm.t[0];
-                    R.x[X_DU] = Sm.t[2];
-                    R.x[X_DV] = p_mul(neg, Sm.t[1]);
-                    R.x[X_DP] = Sm.t[3];
-                    R.x[X_TRHO] = p_mul(neg, Sm.s[0]);
-                    R.x[X_TU] = p_mul(neg, Sm.s[2]);
-                    R.x[X_TV] = Sm.s[1];
-                    R.x[X_TP] = p_mul(neg, Sm.s[3]);
-                    bool ux, uy;
-                    int kx, ky;
-                    strip_face_pair(L, R, G, a.tau, a.htau, YF, ux, uy, kx, ky);
-                    const bool qx = needA && (!ux || kx == 2), qy = needB && (!uy || ky == 2);
-                    if (needA && !qx && kx)
-                        report_face(a.ctl, slot, 1, (unsigned long long)q1 * (n + 1) + cA, kx);
-                    if (needB && !qy && ky)
-                        report_face(a.ctl, slot, 1, (unsigned long long)q1 * (n + 1) + cB, ky);
-                    strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, ownA, ownB, true, q1, cA, q1, cB, a,
-                                         M, stats3, YF);
-                }
-                // update of row r-1: x-faces r-1 (XFm) and r (XF0), y-faces A, B and the next lane's A
-                float2 Ar[8];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    Ar[t] = make_float2(YF.F[t].y, __shfl_down_sync(FULL, YF.F[t].x, 1));
-                    Ar[4 + t] = make_float2(YF.I[t].y, __shfl_down_sync(FULL, YF.I[t].x, 1));
-                }
-                if (upd_x || upd_y) {
-                    const float2 nu = p_s(a.nu), mu = p_s(a.mu);
-                    // y-face fluxes in the global frame: x-momentum -Ft, y-momentum Fn
-                    const float2 dFx0 = p_sub(XF0.F[0], XFm.F[0]), dFy0 = p_sub(Ar[0], YF.F[0]);
-                    const float2 dFx1 = p_sub(XF0.F[1], XFm.F[1]), dFy1 = p_sub(YF.F[2], Ar[2]);  // -(Ft_r - Ft_l)
-                    const float2 dFx2 = p_sub(XF0.F[2], XFm.F[2]), dFy2 = p_sub(Ar[1], YF.F[1]);
-                    const float2 dFx3 = p_sub(XF0.F[3], XFm.F[3]), dFy3 = p_sub(Ar[3], YF.F[3]);
-                    const float2 rho = Vm.w[0];
-                    const float2 mom_x = p_sub(p_sub(p_mul(rho, Vm.w[1]), p_mul(nu, dFx1)), p_mul(mu, dFy1));
-                    const float2 mom_y = p_sub(p_sub(p_mul(rho, Vm.w[2]), p_mul(nu, dFx2)), p_mul(mu, dFy2));
-                    const float2 ene = p_sub(p_sub(p_mul(rho, E), p_mul(nu, dFx3)), p_mul(mu, dFy3));
-                    const float2 rn = p_sub(p_sub(rho, p_mul(nu, dFx0)), p_mul(mu, dFy0));
-                    const float2 irn = p_rcp(rn);
-                    const float2 un = p_mul(mom_x, irn), vn = p_mul(mom_y, irn), En2 = p_mul(ene, irn);
-                    const float2 pn = p_mul(p_sub(p_sub(ene, p_mul(p_mul(p_s(0.5f), mom_x), un)), p_mul(p_mul(p_s(0.5f), mom_y), vn)),
-                                            p_s(G.gm1));
-                    if ((upd_x && (pn.x < G.eps || rn.x < G.eps)) || (upd_y && (pn.y < G.eps || rn.y < G.eps)))
-                        bad = 1u;
-                    float2 ns[4], nt[4];
-                    const float2 ihx2 = p_s(ihx), ihy2 = p_s(ihy);
-#pragma unroll
-                    for (int t = 0; t < 4; ++t)
-                        ns[t] = p_mul(p_sub(XF0.I[t], XFm.I[t]), ihx2);
-                    // y-face I in the global frame: (I0, -B, A, I3)
-                    nt[0] = p_mul(p_sub(Ar[4], YF.I[0]), ihy2);
-                    nt[1] = p_mul(p_sub(YF.I[2], Ar[6]), ihy2);
-                    nt[2] = p_mul(p_sub(Ar[5], YF.I[1]), ihy2);
-                    nt[3] = p_mul(p_sub(Ar[7], YF.I[3]), ihy2);
-                    const size_t o = (size_t)q1 * a.ld + c;
-                    float* dw = a.dst_w + o;
-                    if (upd_x && upd_y) {
-                        *reinterpret_cast<float2*>(dw) = rn;
-                        *reinterpret_cast<float2*>(dw + a.plane) = un;
-                        *reinterpret_cast<float2*>(dw + 2 * a.plane) = vn;
-                        *reinterpret_cast<float2*>(dw + 3 * a.plane) = pn;
-                        *reinterpret_cast<float2*>(dw + 4 * a.plane) = En2;
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) {
-                            *reinterpret_cast<float2*>(a.dst_s + t * a.plane + o) = ns[t];
-                            *reinterpret_cast<float2*>(a.dst_t + t * a.plane + o) = nt[t];
-                        }
-                    } else {  // upd_x only (the last column of the domain is this pair's first)
-                        dw[0] = rn.x;
-                        dw[a.plane] = un.x;
-                        dw[2 * a.plane] = vn.x;
-                        dw[3 * a.plane] = pn.x;
-                        dw[4 * a.plane] = En2.x;
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) {
-                            a.dst_s[t * a.plane + o] = ns[t].x;
-                            a.dst_t[t * a.plane + o] = nt[t].x;
-                        }
-                    }
-                }
-            }
-            // advance
-            Vm = V0;
-            V0 = Vp;
-            Vp = Vn;
-            Sm = S0;
-            P = Pn;
-            XFm = XF0;
-            E = En;
-        }
+        const int r0 = seg * sa.seg;
+        strip_unit<LEARNED>(a, strip * STRIP_W, r0, (r0 + sa.seg < a.m) ? r0 + sa.seg : a.m, q, M, stats3, bad);
     }
-    if (__any_sync(FULL, bad != 0u) && lane == 0)
-        atomicOr(&a.ctl->upd_bad[slot], 1u);
-    if (a.stats) {
-        for (int off = 16; off; off >>= 1) {
-            stats3[0] += __shfl_xor_sync(FULL, stats3[0], off);
-            stats3[1] += __shfl_xor_sync(FULL, stats3[1], off);
-            stats3[2] += __shfl_xor_sync(FULL, stats3[2], off);
-        }
-        if (lane == 0 && stats3[0]) {
-            atomicAdd(&a.ctl->newton_faces, (unsigned long long)stats3[0]);
-            atomicAdd(&a.ctl->newton_iters, (unsigned long long)stats3[1]);
-            if (stats3[2])
-                atomicAdd(&a.ctl->newton_fallbacks, (unsigned long long)stats3[2]);
-        }
-    }
+    strip_report(a.ctl, a.seq % 3, a.stats, stats3, bad);
 }
 
 }  // namespace hydro
