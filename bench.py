@@ -58,6 +58,17 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def fp64_inst_per_cell():
+    """FP64-pipe thread instructions per cell-update of the FP64 step kernel
+    (ncu capture summarised in profiles/traffic.json), and that kernel."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            d = json.load(f)["fp64"]
+        return float(d["fp64_thread_inst_per_cell"]), d["kernel"]
+    except Exception:
+        return None, None
+
+
 def traffic_per_cell(form_key):
     """DRAM bytes per cell-update of a form's step kernel from the committed
     ncu summary, and the kernel configuration it was captured on."""
@@ -588,6 +599,19 @@ def main():
     if fp64:
         fp64_short = {"value": fp64["value"], "ms_per_step": fp64["ms_per_step"], "steps": k64,
                       "kernel_variant": fp64["kernel_variant"], "hbm_frac": forms["fp64"]["hbm_frac"]}
+        # the FP64 form is bound by the FP64 pipe: its roofline is the FP64
+        # instructions per cell (ncu) times the cell rate against the measured DFMA rate
+        try:
+            pk = hg.fp64_peak()
+        except Exception:
+            pk = None
+        ipc, ik = fp64_inst_per_cell()
+        fp64_short["fp64_pipe_roofline"] = {
+            "bound": "fp64 pipe", "peak": pk, "unit": "FP64 thread-instructions/s",
+            "peak_source": "measured (hydro_fp64_peak: DFMA chains on every SM)",
+            "inst_per_cell": ipc, "inst_source": f"ncu capture of {ik} at 2048^2 (profiles/traffic.json)" if ipc else None,
+            "achieved": ipc * fp64["value"] if ipc else None,
+            "frac": ipc * fp64["value"] / pk if (ipc and pk) else None}
     learned = {"ms_per_step": head["ms_per_step"], "plain_fp32_ms_per_step": plain["ms_per_step"],
                "speedup_over_plain_fp32": plain["ms_per_step"] / head["ms_per_step"],
                "speedup_over_fp64": forms["speedup_learned_over_fp64"],

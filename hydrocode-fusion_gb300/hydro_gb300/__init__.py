@@ -402,6 +402,16 @@ def features(states, gamma=1.4):
     return X
 
 
+def fp64_peak() -> float:
+    """Measured FP64 fused multiply-add rate of the current GPU (DFMA/s)."""
+    v = ctypes.c_double()
+    L = lib()
+    L.hydro_fp64_peak.restype = ctypes.c_int
+    if L.hydro_fp64_peak(ctypes.byref(v)) != 0:
+        raise RuntimeError("hydro_fp64_peak failed: " + last_error())
+    return float(v.value)
+
+
 def load_weights(path: str = WEIGHTS_PATH) -> np.ndarray:
     w = np.fromfile(path, dtype="<f4")
     if w.size != MLP_NPARAM:

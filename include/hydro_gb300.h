@@ -169,6 +169,10 @@ int hydro2d_autotune(hydro2d_t *h, const double *cfg, int ncfg, int steps, float
  * copies its result words to the host and waits for its stream. */
 int hydro1d_run_noalloc(int m, double *d_state, const double *cfg, int ncfg, int order, void *stream,
                         hydro_run_info *info);
+/* Measured FP64 fused multiply-add rate of the current GPU (DFMA per second,
+ * all SMs, no memory traffic): the FP64 pipe's peak for the roofline of the
+ * FP64 form (no reference counterpart). */
+int hydro_fp64_peak(double *dfma_per_s);
 /* ---- learned Newton starting pressure (no reference counterpart) ---------
  * A 6-64-64-1 ReLU network predicting log(p_star / sqrt(pL pR)) of a Riemann problem
  * from scale-free features; trained on the GPU by this library's own
