@@ -1,7 +1,7 @@
 // solver2d_f64.cu -- FP64 (parity) instantiation of the 2D solver.
 // Compiled with --fmad=false: no multiply-add contraction, IEEE division and
-// square root, so every operation rounds exactly as the reference's C code
-// (only pow() differs from glibc's, by at most a couple of ulp).
+// square root, so every operation rounds exactly as the reference's C code,
+// pow() included (libm_pow.cuh follows the C library's own method).
 #include "solver2d_impl.cuh"
 
 namespace hydro {
