@@ -1,11 +1,15 @@
 // batch.cu -- many independent 2D problems of uneven grid size advanced together.
 //
-// Every problem keeps its own two-state buffer (the one-problem layout: 26
-// pitched planes), boundary table, time step and halting control block.  All
-// tiles of all problems form one flat work list, and every tile runs exactly
-// the per-tile code of the one-problem FP32 step (unsplit_tile), so each
-// problem's result is a one-problem FP32 run of the same data (to the last
-// bit where the same compiled instance runs; separately compiled kernels may
+// Every problem keeps its own two states (13 pitched planes each), boundary
+// table, time step and halting control block.  The planes are pooled: plane k
+// of state s of every problem lies in one array of `pool` elements, problem p
+// at offset off[p], so the stride between a problem's planes is the same for
+// all problems.  All work units of all problems form one flat list; a unit is
+// a tile running exactly the per-tile code of the one-problem FP32 step
+// (unsplit_tile), or, for the strip shapes, a (strip, run of rows) running the
+// one-problem strip kernel's per-unit march (strip_unit).  Each problem's
+// result is therefore a one-problem FP32 run of the same data (to the last bit
+// where the same compiled instance runs; separately compiled kernels may
 // contract multiply-adds differently under fast math, a difference at FP32
 // rounding).  There is no reference counterpart: the reference advances one grid
 // per process (grp_solver_2D_EUL_source.c:146-286).
@@ -15,7 +19,8 @@
 //   1  persistent, static round robin over a largest-problem-first order
 //   2  persistent, dynamic (one atomic work counter per step), problem-major
 //   3  persistent, dynamic, largest-first
-//   4  a CUDA graph of one launch per step, one CTA per tile
+//   4  a CUDA graph of one launch per step, one CTA per tile (strip shapes:
+//      the CTAs that fit at once, taking units from the step's counter)
 // "Persistent" is ONE cooperative kernel for all steps with a grid barrier
 // between steps; its wait is bounded by the global timer (the barrier gives
 // up, flags an error and every CTA returns).  The launch is captured in a
@@ -26,6 +31,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <numeric>
 #include <vector>
 
@@ -193,24 +199,222 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_step(const __grid_constant__
     batch_tile<TJ, TI, NT>(B, B.order[blockIdx.x], step, sa, smem_raw, M);
 }
 
+// ---------------------------------------------------------------------------
+// strip shapes: the one-grid strip kernel's per-unit march (strip_unit), a
+// unit being (problem, strip of 60 columns, SEG rows)
+// ---------------------------------------------------------------------------
+// Per problem, what a strip unit needs beyond the batch's common arguments
+// (56 B, so that the arguments of BATCH_STRIP_MAX problems fit the kernel's
+// parameter space, from which a warp-uniform problem index reads them).
+constexpr int BATCH_STRIP_MAX = 576;
+struct BatchStripProb {
+    unsigned off64;  // element offset of the problem's planes within each plane of the pool, / 64
+    unsigned spare;
+    unsigned goff;   // element offset of its boundary table
+    int m, n, ld;
+    float tau, hx, hy, inv_hx, inv_hy, nu, mu;
+    int pow2;  // bit 0: h_x is a power of two, bit 1: h_y
+};
+static_assert(sizeof(BatchStripProb) == 56, "per-problem strip arguments");
+
+struct BatchStripDev {
+    BatchDev B;
+    float* mem;          // plane k of state s of every problem starts at mem + (13 s + k) pool
+    size_t pool;
+    const float* ghost;
+    float alpha;
+    int bx, by;
+    BatchStripProb P[BATCH_STRIP_MAX];
+};
+static_assert(sizeof(BatchStripDev) <= 32764, "kernel parameter space");
+
+// The members of StepArgs<float> that strip_unit reads, for one problem and step.
+struct BatchStripView {
+    int m, n, ld;
+    size_t plane;
+    const float* src_w;
+    float* dst_w;
+    const float* src_s;
+    float* dst_s;
+    const float* src_t;
+    float* dst_t;
+    const float* ghost0;
+    float tau, htau, hx, hy, hhx, hhy, inv_hx, inv_hy;
+    int pow2_x, pow2_y;
+    float nu, mu, alpha;
+    int bx, by, find_x, find_y;
+    Ctl* ctl;
+    int seq, stats;
+};
+
+// One unit e of the flat unit list at step `step` (warp-collective): the
+// problem's halting protocol (as batch_tile_args), then strip_unit.
+template <int SEG>
+__device__ __forceinline__ void batch_strip_unit(const BatchStripDev& D, int e, int step, float* q, int* stats3)
+{
+    const BatchDev& B = D.B;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    // the unit's problem and local index, warp-uniform by construction
+    const int p = (int)__reduce_max_sync(FULL, (unsigned)B.tile_prob[e]);
+    const int lt = (int)__reduce_max_sync(FULL, (unsigned)B.tile_local[e]);
+    volatile Ctl* c = B.ctl + p;
+    bool ok = c->halted_seq == 0;
+    if (ok && step > 1) {
+        const int ps = (step - 1) % 3;
+        const int d = halt_decision(c->key[ps][0], c->key[ps][1], c->upd_bad[ps]);
+        if (d) {
+            ok = false;
+            if (lt == 0 && lane == 0) {
+                c->halt_kind = d;
+                c->halted_seq = step - 1;
+            }
+        }
+    }
+    if (!ok)
+        return;
+    if (lt == 0 && lane == 0) {
+        const int ns = (step + 1) % 3;
+        c->key[ns][0] = 0ull;
+        c->key[ns][1] = 0ull;
+        c->upd_bad[ns] = 0u;
+    }
+    const BatchStripProb& P = D.P[p];
+    BatchStripView a;
+    a.m = P.m;
+    a.n = P.n;
+    a.ld = P.ld;
+    a.plane = D.pool;
+    // odd steps read state 0 and write state 1, even steps the reverse
+    const size_t o = (size_t)P.off64 * 64;
+    float* W0 = D.mem + ((step & 1) ? 0 : 13 * D.pool) + o;
+    float* W1 = D.mem + ((step & 1) ? 13 * D.pool : 0) + o;
+    a.src_w = W0;
+    a.dst_w = W1;
+    a.src_s = W0 + 5 * a.plane;
+    a.dst_s = W1 + 5 * a.plane;
+    a.src_t = W0 + 9 * a.plane;
+    a.dst_t = W1 + 9 * a.plane;
+    a.ghost0 = D.ghost + P.goff;
+    a.tau = P.tau;
+    a.htau = 0.5f * P.tau;
+    a.hx = P.hx;
+    a.hy = P.hy;
+    a.hhx = 0.5f * P.hx;
+    a.hhy = 0.5f * P.hy;
+    a.inv_hx = P.inv_hx;
+    a.inv_hy = P.inv_hy;
+    a.pow2_x = P.pow2 & 1;
+    a.pow2_y = (P.pow2 >> 1) & 1;
+    a.nu = P.nu;
+    a.mu = P.mu;
+    a.alpha = D.alpha;
+    a.bx = D.bx;
+    a.by = D.by;
+    a.find_x = a.find_y = (step > 1);
+    a.ctl = B.ctl + p;
+    a.seq = step;
+    a.stats = B.stats;
+    const int nstrip = (a.n + STRIP_W - 1) / STRIP_W;
+    const int seg = lt / nstrip, strip = lt - seg * nstrip;
+    const int r0 = seg * SEG;
+    unsigned bad = 0;
+    strip_unit<false>(a, &B.G, strip * STRIP_W, r0, (r0 + SEG < a.m) ? r0 + SEG : a.m, q, nullptr, stats3, bad);
+    strip_report(a.ctl, step % 3, B.stats, stats3, bad);
+}
+
+// ONE cooperative kernel for all steps of all problems, strip units; warps
+// take units by a static stride or from the step's counter (one call site of
+// the unit code for both).
+template <int NW, int SEG>
+__global__ void __launch_bounds__(NW * 32, 1) k_batch_strip_persistent(const __grid_constant__ BatchStripDev D)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const BatchDev& B = D.B;
+    const unsigned FULL = 0xffffffffu;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* q = reinterpret_cast<float*>(smem_raw + warp * StripSmem<NW, false>::q_bytes);
+    int stats3[3] = {0, 0, 0};
+    const int gw = blockIdx.x * NW + warp, nw = gridDim.x * NW;
+    for (int step = 1; step <= B.steps; ++step) {
+        unsigned int* ctr = B.work + (step & 1);
+        int k = gw;
+        for (;;) {
+            if (B.dynamic) {
+                int t = 0;
+                if (lane == 0)
+                    t = (int)atomicAdd(ctr, 1u);
+                k = __shfl_sync(FULL, t, 0);
+            }
+            if (k >= B.ntiles)
+                break;
+            batch_strip_unit<SEG>(D, B.order[k], step, q, stats3);
+            k += nw;
+        }
+        // the counter of the next step was last used two steps ago: reset it
+        if (B.dynamic && blockIdx.x == 0 && threadIdx.x == 0)
+            B.work[(step + 1) & 1] = 0u;
+        if (!grid_barrier(B))
+            return;
+    }
+}
+
+// One step of all problems, strip units from the step's counter (the per-step
+// graph schedule; a grid of the CTAs that fit at once).
+template <int NW, int SEG>
+__global__ void __launch_bounds__(NW * 32, 1) k_batch_strip_step(const __grid_constant__ BatchStripDev D, int step)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const BatchDev& B = D.B;
+    const unsigned FULL = 0xffffffffu;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* q = reinterpret_cast<float*>(smem_raw + warp * StripSmem<NW, false>::q_bytes);
+    int stats3[3] = {0, 0, 0};
+    unsigned int* ctr = B.work + (step & 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        B.work[(step + 1) & 1] = 0u;  // the next launch's counter (this one's was cleared by the previous launch)
+    for (;;) {
+        int k = 0;
+        if (lane == 0)
+            k = (int)atomicAdd(ctr, 1u);
+        k = __shfl_sync(FULL, k, 0);
+        if (k >= B.ntiles)
+            break;
+        batch_strip_unit<SEG>(D, B.order[k], step, q, stats3);
+    }
+}
+
 struct BatchShape {
-    int TJ, TI, NT, MINB;
+    int TJ, TI, NT, MINB;  // strip shapes: TJ rows per unit, TI = STRIP_W columns
     size_t smem;
     const void* persistent;
     const void* step;
+    int strip;  // 1: strip units (BatchStripDev arguments)
+    int carve;  // shared-memory carveout, percent
 };
 
 template <int TJ, int TI, int NT, int MINB>
 BatchShape batch_shape()
 {
     return BatchShape{TJ, TI, NT, MINB, UnsplitSmem<float, TJ, TI>::bytes,
-                      (const void*)k_batch_persistent<TJ, TI, NT, MINB>, (const void*)k_batch_step<TJ, TI, NT, MINB>};
+                      (const void*)k_batch_persistent<TJ, TI, NT, MINB>, (const void*)k_batch_step<TJ, TI, NT, MINB>,
+                      0, 100};
+}
+
+template <int NW, int SEG>
+BatchShape batch_strip_shape()
+{
+    // the smallest shared-memory configuration that holds two CTAs (64 KB);
+    // the rest of the unified storage is L1 for the strip code's spills
+    return BatchShape{SEG, STRIP_W, NW * 32, 1, StripSmem<NW, false>::bytes,
+                      (const void*)k_batch_strip_persistent<NW, SEG>, (const void*)k_batch_strip_step<NW, SEG>, 1, 28};
 }
 
 static const std::vector<BatchShape>& batch_shapes()
 {
     static const std::vector<BatchShape> s = {batch_shape<32, 32, 512, 1>(), batch_shape<8, 32, 256, 3>(),
-                                              batch_shape<16, 16, 256, 4>()};
+                                              batch_shape<16, 16, 256, 4>(), batch_strip_shape<4, 16>(),
+                                              batch_strip_shape<4, 32>()};
     return s;
 }
 
@@ -239,9 +443,12 @@ struct hydro_batch {
     double wait_s = 5.0;
     std::vector<double> tau;
     std::vector<int> final_buf, halted_kind, halted_step;
+    std::vector<BatchStripProb> sprob;  // per-problem arguments of the strip shapes
 
-    float* W(int p, int buf) { return mem + off[p] + (size_t)buf * 13 * m[p] * ld[p]; }
-    size_t plane(int p) const { return (size_t)m[p] * ld[p]; }
+    size_t pool = 0;  // elements of one plane of all problems: plane k of state s of problem p
+                      // starts at mem + (13 s + k) pool + off[p]
+    float* W(int p, int buf) { return mem + (size_t)buf * 13 * pool + off[p]; }
+    size_t plane(int) const { return pool; }  // the stride between a problem's planes
     int grid1d(size_t total) const
     {
         size_t b = (total + 255) / 256, cap = (size_t)sms * 8;
@@ -275,6 +482,7 @@ static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps,
     rc.t_all = INFINITY;  // fixed step count
     std::vector<StepArgs<float>> args(BATCH_VERSIONS * (size_t)np);
     b->tau.assign(np, 0.0);
+    b->sprob.assign(np, BatchStripProb{});
     for (int p = 0; p < np; ++p) {
         const int m = b->m[p], n = b->n[p], ld = b->ld[p];
         const size_t plane = b->plane(p);
@@ -307,6 +515,23 @@ static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps,
                 return -1;
             }
         b->tau[p] = r0.tau_face;
+        {
+            // the same values as the step arguments below
+            BatchStripProb& sp = b->sprob[p];
+            sp.off64 = (unsigned)(b->off[p] / 64);
+            sp.goff = (unsigned)b->goff[p];
+            sp.m = m;
+            sp.n = n;
+            sp.ld = ld;
+            sp.tau = (float)r0.tau_face;
+            sp.hx = (float)r.hx;
+            sp.hy = (float)r.hy;
+            sp.inv_hx = (float)(1.0 / r.hx);
+            sp.inv_hy = (float)(1.0 / r.hy);
+            sp.nu = (float)r0.fac_x;
+            sp.mu = (float)r0.fac_y;
+            sp.pow2 = (h_is_pow2(r.hx) ? 1 : 0) | (h_is_pow2(r.hy) ? 2 : 0);
+        }
         for (int ver = 0; ver < BATCH_VERSIONS; ++ver) {
             // a representative step of this version (same parity, slot and first-step flag)
             int step = 1;
@@ -398,12 +623,32 @@ static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps,
 }
 
 // Records the time loop of the current schedule on the (capturing) stream.
-static int batch_enqueue(hydro_batch* b, const BatchShape& S, BatchDev& B, int steps)
+// kp: the kernels' argument, a BatchDev or (strip shapes) a BatchStripDev.
+static int batch_enqueue(hydro_batch* b, const BatchShape& S, const BatchDev& B, void* kp, int steps)
 {
-    if (b->schedule == 4) {
+    if (b->schedule == 4 && !S.strip) {
         for (int s = 1; s <= steps; ++s) {
-            void* kargs[] = {(void*)&B, (void*)&s};
+            void* kargs[] = {kp, (void*)&s};
             if (!cuda_ok(cudaLaunchKernel(S.step, dim3(B.ntiles), dim3(S.NT), kargs, S.smem, b->stream),
+                         "batch step launch"))
+                return -1;
+        }
+        count_launch(steps);
+        return 0;
+    }
+    const int nwarps = S.NT / 32;
+    if (b->schedule == 4) {  // strip units: per step, the CTAs that fit at once take units from a counter
+        int per_sm = 0;
+        if (!cuda_ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, S.step, S.NT, S.smem), "occupancy"))
+            return -1;
+        if (per_sm < 1) {
+            set_error("batch: the step kernel does not fit on an SM");
+            return -1;
+        }
+        const int grid = std::max(1, std::min(per_sm * b->sms, (B.ntiles + nwarps - 1) / nwarps));
+        for (int s = 1; s <= steps; ++s) {
+            void* kargs[] = {kp, (void*)&s};
+            if (!cuda_ok(cudaLaunchKernel(S.step, dim3(grid), dim3(S.NT), kargs, S.smem, b->stream),
                          "batch step launch"))
                 return -1;
         }
@@ -417,7 +662,8 @@ static int batch_enqueue(hydro_batch* b, const BatchShape& S, BatchDev& B, int s
         set_error("batch: the persistent kernel does not fit on an SM");
         return -1;
     }
-    const int grid = std::min(per_sm * b->sms, B.ntiles);
+    const int work_ctas = S.strip ? (B.ntiles + nwarps - 1) / nwarps : B.ntiles;
+    const int grid = std::max(1, std::min(per_sm * b->sms, work_ctas));
     cudaLaunchConfig_t lc;
     memset(&lc, 0, sizeof(lc));
     lc.gridDim = dim3(grid);
@@ -429,7 +675,7 @@ static int batch_enqueue(hydro_batch* b, const BatchShape& S, BatchDev& B, int s
     at[0].val.cooperative = 1;
     lc.attrs = at;
     lc.numAttrs = 1;
-    void* kargs[] = {(void*)&B};
+    void* kargs[] = {kp};
     if (!cuda_ok(cudaLaunchKernelExC(&lc, S.persistent, kargs), "batch persistent launch"))
         return -1;
     count_launch();
@@ -461,15 +707,16 @@ int hydro_batch_create(hydro_batch** out, int nprob, const int* m, const int* n)
         }
         b->ld[p] = (n[p] + 31) / 32 * 32;
         // 256-byte aligned starts keep every problem's stations 128-byte aligned
-        b->off[p + 1] = b->off[p] + ((size_t)26 * m[p] * b->ld[p] + 63) / 64 * 64;
+        b->off[p + 1] = b->off[p] + ((size_t)m[p] * b->ld[p] + 63) / 64 * 64;
         b->goff[p + 1] = b->goff[p] + 8 * ((size_t)m[p] + n[p]);
         maxmn = std::max(maxmn, (size_t)m[p] * n[p]);
     }
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
-    if (!cuda_ok(cudaMalloc(&b->mem, sizeof(float) * b->off[nprob]), "batch states") ||
-        !cuda_ok(cudaMemset(b->mem, 0, sizeof(float) * b->off[nprob]), "batch clear") ||
+    b->pool = b->off[nprob];
+    if (!cuda_ok(cudaMalloc(&b->mem, sizeof(float) * 26 * b->pool), "batch states") ||
+        !cuda_ok(cudaMemset(b->mem, 0, sizeof(float) * 26 * b->pool), "batch clear") ||
         !cuda_ok(cudaMalloc(&b->ghost, sizeof(float) * b->goff[nprob]), "batch boundary tables") ||
         !cuda_ok(cudaMalloc(&b->ctl, sizeof(Ctl) * nprob), "batch control blocks") ||
         !cuda_ok(cudaMalloc(&b->args, sizeof(StepArgs<float>) * BATCH_VERSIONS * nprob), "batch step arguments") ||
@@ -485,7 +732,7 @@ int hydro_batch_create(hydro_batch** out, int nprob, const int* m, const int* n)
         for (const void* k : {s.persistent, s.step})
             if (!cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem),
                          "smem attr") ||
-                !cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100),
+                !cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, s.carve),
                          "carveout attr")) {
                 delete b;
                 return -1;
@@ -523,8 +770,12 @@ int hydro_batch_upload(hydro_batch* b, int p, const double* rho, const double* u
         k_pack_plane<float><<<b->grid1d(mn), 256, 0, b->stream>>>(st + k * mn, b->W(p, 0) + k * plane, m, n, ld);
         count_launch();
     }
-    if (!cuda_ok(cudaMemsetAsync(b->W(p, 0) + 5 * plane, 0, sizeof(float) * 8 * plane, b->stream), "batch clear") ||
-        !cuda_ok(cudaMemsetAsync(b->W(p, 1) + 5 * plane, 0, sizeof(float) * 8 * plane, b->stream), "batch clear"))
+    // the 8 slope planes of both states: rows of m ld elements, pool elements apart
+    const size_t row = sizeof(float) * m * ld;
+    if (!cuda_ok(cudaMemset2DAsync(b->W(p, 0) + 5 * plane, sizeof(float) * plane, 0, row, 8, b->stream),
+                 "batch clear") ||
+        !cuda_ok(cudaMemset2DAsync(b->W(p, 1) + 5 * plane, sizeof(float) * plane, 0, row, 8, b->stream),
+                 "batch clear"))
         return -1;
     if (!b->final_buf.empty())
         b->final_buf[p] = 0;
@@ -556,6 +807,14 @@ int hydro_batch_download(hydro_batch* b, int p, double* rho, double* u, double* 
 }
 
 int hydro_batch_num_shapes(void) { return (int)batch_shapes().size(); }
+int hydro_batch_shape_kind(int shape)
+{
+    if (shape < 0 || shape >= (int)batch_shapes().size()) {
+        set_error("batch: no such tile shape");
+        return -1;
+    }
+    return batch_shapes()[shape].strip;
+}
 int hydro_batch_num_schedules(void) { return BATCH_SCHEDULES; }
 
 int hydro_batch_shape(int shape, int* out4)
@@ -604,6 +863,10 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
         return -1;
     }
     const BatchShape& S = batch_shapes()[b->shape];
+    if (S.strip && (b->nprob > BATCH_STRIP_MAX || b->pool / 64 > 0xffffffffull || b->goff[b->nprob] > 0xffffffffull)) {
+        set_error("batch: the strip shapes take at most 576 problems of at most 2^38 state elements");
+        return -1;
+    }
     int nt = 0;
     if (batch_prepare(b, cfg, ncfg, steps, stats, S, b->schedule, &nt))
         return -1;
@@ -625,9 +888,23 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
     B.bar_gen = b->sync + 3;
     B.bar_err = (int*)(b->sync + 4);
     B.wait_ns = (unsigned long long)(b->wait_s * 1e9);
-    {
-        const RunConfig rc = run_config_from(cfg, ncfg);
-        fill_gas_params(B.G, rc.gamma, rc.eps);
+    const RunConfig rcfg = run_config_from(cfg, ncfg);
+    fill_gas_params(B.G, rcfg.gamma, rcfg.eps);
+    // the strip shapes' arguments: the batch's common ones and every problem's
+    std::unique_ptr<BatchStripDev> D;
+    void* kp = &B;
+    if (S.strip) {
+        D.reset(new BatchStripDev());
+        memset(D.get(), 0, sizeof(BatchStripDev));
+        D->B = B;
+        D->mem = b->mem;
+        D->pool = b->pool;
+        D->ghost = b->ghost;
+        D->alpha = (float)rcfg.alpha;
+        D->bx = rcfg.bx;
+        D->by = rcfg.by;
+        std::copy(b->sprob.begin(), b->sprob.end(), D->P);
+        kp = D.get();
     }
     if (!cuda_ok(cudaMemsetAsync(b->ctl, 0, sizeof(Ctl) * b->nprob, b->stream), "batch control clear") ||
         !cuda_ok(cudaMemsetAsync(b->sync, 0, sizeof(unsigned int) * 8, b->stream), "batch barrier clear"))
@@ -638,7 +915,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
     cudaGraphExec_t exec = nullptr;
     int graphed = 0;
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        const int rc = batch_enqueue(b, S, B, steps);
+        const int rc = batch_enqueue(b, S, B, kp, steps);
         const cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
         if (rc == 0 && ce == cudaSuccess && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
             graphed = 1;
@@ -657,7 +934,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
     if (graphed)
         rc = cuda_ok(cudaGraphLaunch(exec, b->stream), "batch graph launch") ? 0 : -1;
     else
-        rc = batch_enqueue(b, S, B, steps);
+        rc = batch_enqueue(b, S, B, kp, steps);
     cudaEventRecord(b->e1, b->stream);
     std::vector<Ctl> hc(b->nprob);
     unsigned int hs[8] = {0};
@@ -721,7 +998,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
 
 int hydro_batch_autotune(hydro_batch* b, const double* cfg, int ncfg, int steps, float* times_ms)
 {
-    const size_t total = b->off[b->nprob];
+    const size_t total = 26 * b->pool;
     float* backup = nullptr;
     if (!cuda_ok(cudaMalloc(&backup, sizeof(float) * total), "autotune backup"))
         return -1;

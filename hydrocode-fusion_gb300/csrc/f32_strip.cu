@@ -8,14 +8,20 @@ namespace hydro {
 
 void variants_f32_strip(std::vector<StepVariant<float>>& v, bool learned)
 {
-    // 4 warps per CTA; units of 16 or 32 rows; half of the L1/shared storage
-    // left as L1 for the kernel's register spills
+    // 4 warps per CTA; units of 16 or 32 rows; the L1/shared split: half of
+    // the storage as L1 (for the kernel's register spills and the rows in
+    // flight), or the smallest shared-memory configuration that holds two CTAs
+    // (100 KB with the network image, else 64 KB) and the rest as L1
     if (learned) {
         v.push_back(strip_variant<4, 1, true>(16, 50));
         v.push_back(strip_variant<4, 1, true>(32, 50));
+        v.push_back(strip_variant<4, 1, true>(16, 43));
+        v.push_back(strip_variant<4, 1, true>(32, 43));
     } else {
         v.push_back(strip_variant<4, 1, false>(16, 50));
         v.push_back(strip_variant<4, 1, false>(32, 50));
+        v.push_back(strip_variant<4, 1, false>(16, 28));
+        v.push_back(strip_variant<4, 1, false>(32, 28));
     }
 }
 

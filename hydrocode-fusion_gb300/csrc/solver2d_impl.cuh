@@ -904,8 +904,19 @@ public:
                     sa.work = work;
                     sa.seg = V.TJ;
                     void* args[] = {(void*)&a, (void*)&sa};
-                    if (!cuda_ok(cudaLaunchKernel(V.kern, dim3(sms * V.occ), dim3(V.NT), args, V.smem, stream),
-                                 "step launch"))
+                    // variants of one kernel differ in their L1/shared split: set per launch
+                    cudaLaunchConfig_t lc;
+                    memset(&lc, 0, sizeof(lc));
+                    lc.gridDim = dim3(sms * V.occ);
+                    lc.blockDim = dim3(V.NT);
+                    lc.dynamicSmemBytes = V.smem;
+                    lc.stream = stream;
+                    cudaLaunchAttribute at[1];
+                    at[0].id = cudaLaunchAttributePreferredSharedMemoryCarveout;
+                    at[0].val.sharedMemCarveout = (unsigned)V.carve;
+                    lc.attrs = at;
+                    lc.numAttrs = 1;
+                    if (!cuda_ok(cudaLaunchKernelExC(&lc, V.kern, args), "step launch"))
                         return -1;
                 } else if (V.tma) {
                     // the boxes read the state buffer w, whose slope planes are s = t = w here

@@ -125,8 +125,8 @@ __device__ __forceinline__ bool halt_prologue(Ctl* ctl, int seq)
 // ---------------------------------------------------------------------------
 // boundary-aware load of rho,u,v,p of cell (j, i), possibly a ghost
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ void load_prims(const StepArgs<R>& a, int j, int i, R w[4])
+template <typename R, class A>
+__device__ __forceinline__ void load_prims(const A& a, int j, int i, R w[4])
 {
     const int m = a.m, n = a.n;
     // periodic directions first: a wrapped halo cell is a real cell whose own
@@ -177,8 +177,8 @@ __device__ __forceinline__ void load_prims(const StepArgs<R>& a, int j, int i, R
 
 // Index of a cell for reading its previous slopes (wrapped for periodic
 // boundaries, clamped otherwise: non-periodic ghosts' slopes are overridden).
-template <typename R>
-__device__ __forceinline__ size_t slope_index(const StepArgs<R>& a, int j, int i)
+template <class A>
+__device__ __forceinline__ size_t slope_index(const A& a, int j, int i)
 {
     int jj = j, ii = i;
     if (jj < 0 || jj >= a.m)

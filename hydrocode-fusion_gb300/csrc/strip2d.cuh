@@ -106,7 +106,8 @@ __device__ __forceinline__ float2 strip_limit(float2 wl, float2 wc, float2 wr, f
 // ---------------------------------------------------------------------------
 // loads of one row of the lane's column pair (c, c+1)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void strip_load_vals(const StepArgs<float>& a, int j, int c, bool fast, SV2& V)
+template <class A>
+__device__ __forceinline__ void strip_load_vals(const A& a, int j, int c, bool fast, SV2& V)
 {
     if (fast) {
         const float* b = a.src_w + (size_t)j * a.ld + c;
@@ -123,7 +124,8 @@ __device__ __forceinline__ void strip_load_vals(const StepArgs<float>& a, int j,
     }
 }
 
-__device__ __forceinline__ void strip_load_prev(const StepArgs<float>& a, int j, int c, bool fast, SS2& P)
+template <class A>
+__device__ __forceinline__ void strip_load_prev(const A& a, int j, int c, bool fast, SS2& P)
 {
     if (fast) {
         const size_t o = (size_t)j * a.ld + c;
@@ -144,7 +146,8 @@ __device__ __forceinline__ void strip_load_prev(const StepArgs<float>& a, int j,
 
 // Limited slopes of row r (values Vm, V0, Vp of rows r-1, r, r+1; previous
 // slopes P).  The y-neighbours of the pair come from the adjacent lanes.
-__device__ __forceinline__ void strip_slopes(const StepArgs<float>& a, const SV2& Vm, const SV2& V0, const SV2& Vp,
+template <class A>
+__device__ __forceinline__ void strip_slopes(const A& a, const SV2& Vm, const SV2& V0, const SV2& Vp,
                                              const SS2& P, float ahx, float ihx, float ahy, float ihy, SS2& S)
 {
     const unsigned FULL = 0xffffffffu;
@@ -160,7 +163,8 @@ __device__ __forceinline__ void strip_slopes(const StepArgs<float>& a, const SV2
 
 // Ghost slopes of a non-periodic x-boundary row (bound_cond_slope_limiter_x.c:
 // 94-126, as phase 2b of the tile kernels): from the edge row's slopes E.
-__device__ __forceinline__ void strip_ghost_row(const StepArgs<float>& a, const SS2& E, bool low, SS2& S)
+template <class A>
+__device__ __forceinline__ void strip_ghost_row(const A& a, const SS2& E, bool low, SS2& S)
 {
     const bool keep_su = (a.bx == -2) || (a.bx == -24 && low);
     S.s[0] = make_float2(0.f, 0.f);
@@ -175,7 +179,8 @@ __device__ __forceinline__ void strip_ghost_row(const StepArgs<float>& a, const 
 // Ghost slopes of the non-periodic y-boundary columns -1 and n of a row
 // (bound_cond_slope_limiter_y.c:94-126): the edge column's slopes by the
 // same rules.  Warp-collective; c = first column of the lane's pair.
-__device__ __forceinline__ void strip_ghost_cols(const StepArgs<float>& a, int c, SS2& S)
+template <class A>
+__device__ __forceinline__ void strip_ghost_cols(const A& a, int c, SS2& S)
 {
     const unsigned FULL = 0xffffffffu;
     const int n = a.n;
@@ -322,13 +327,23 @@ __device__ __forceinline__ void strip_put_side(float* e, const SSide2& S, bool y
         e[k] = y ? S.x[k].y : S.x[k].x;
 }
 
+// What a flush needs of its grid: the gas (in the kernel's parameter space),
+// the face time step, the control block and launch slot of the error keys, the
+// grid's size for the keys' serial numbers.
+struct StripFlushArgs {
+    const Gas<float>* G;
+    Ctl* ctl;
+    float tau, htau;
+    int m, n, slot;
+};
+
 template <bool LEARNED>
-static __device__ __noinline__ void strip_flush(float* q, int cnt, const StepArgs<float>* ap, const MlpShared* M,
+static __device__ __noinline__ void strip_flush(float* q, int cnt, const StripFlushArgs fa, const MlpShared* M,
                                                 int* stats3)
 {
-    const StepArgs<float>& a = *ap;
+    const Gas<float>& G = *fa.G;
     const int lane = threadIdx.x & 31;
-    const int slot = a.seq % 3;
+    const int slot = fa.slot;
     for (int base = 0; base < cnt; base += 32) {
         const int k = base + lane;
         const bool act = k < cnt;
@@ -347,7 +362,7 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StepArg
         float p_start = -1.f;
         if constexpr (LEARNED) {
             if (cnt - base >= STRIP_MLP_MIN)  // warp-uniform
-                p_start = learned_guess(L, Rr, act && !retry, a.G, *M, cnt - base < 32 ? cnt - base : 32);
+                p_start = learned_guess(L, Rr, act && !retry, G, *M, cnt - base < 32 ? cnt - base : 32);
         }
         if (!act)
             continue;
@@ -355,7 +370,7 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StepArg
         int code;
         if (!retry) {
             int it = 0, fb = 0;
-            code = solve_face<float, 2, 0>(L, Rr, a.G, a.tau, a.htau, o, it, fb, ydir, p_start);
+            code = solve_face<float, 2, 0>(L, Rr, G, fa.tau, fa.htau, o, it, fb, ydir, p_start);
             if (counted && it >= 0) {
                 stats3[0] += 1;
                 stats3[1] += it;
@@ -365,11 +380,11 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StepArg
             code = 2;
         }
         if (code == 2)
-            code = solve_face_fp64_retry<0>(L, Rr, a.G.g64, a.G.eps64, (double)a.tau, ydir, o);
+            code = solve_face_fp64_retry<0>(L, Rr, G.g64, G.eps64, (double)fa.tau, ydir, o);
         if (!ydir)
-            report_face(a.ctl, slot, 0, (unsigned long long)col * (a.m + 1) + row, code);
+            report_face(fa.ctl, slot, 0, (unsigned long long)col * (fa.m + 1) + row, code);
         else
-            report_face(a.ctl, slot, 1, (unsigned long long)row * (a.n + 1) + col, code);
+            report_face(fa.ctl, slot, 1, (unsigned long long)row * (fa.n + 1) + col, code);
         // back to the normal frame of the strip's outputs (a y-face's global
         // F = (F0, -Ft, Fn, F3), I = (I0, -B, A, I3))
         if (!ydir) {
@@ -390,7 +405,7 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StepArg
 template <bool LEARNED>
 __device__ __forceinline__ void strip_queue(float* q, const SSide2& L, const SSide2& R, bool need_x, bool need_y,
                                             bool retry_x, bool retry_y, bool cnt_x, bool cnt_y, bool ydir, int row_x,
-                                            int col_x, int row_y, int col_y, const StepArgs<float>& a,
+                                            int col_x, int row_y, int col_y, const StripFlushArgs& fa,
                                             const MlpShared* M, int* stats3, SF2& o)
 {
     const unsigned FULL = 0xffffffffu;
@@ -418,7 +433,7 @@ __device__ __forceinline__ void strip_queue(float* q, const SSide2& L, const SSi
         e[26] = __int_as_float((ydir ? 1 : 0) | (retry_y ? 2 : 0) | (cnt_y ? 4 : 0));
     }
     __syncwarp();
-    strip_flush<LEARNED>(q, cnt, &a, M, stats3);
+    strip_flush<LEARNED>(q, cnt, fa, M, stats3);
     __syncwarp();
     if (need_x) {
         const float* e = q + (size_t)ix * STRIP_QWORDS;
@@ -455,17 +470,20 @@ struct StripSmem {
 };
 
 // One work unit of a step: columns [c0, c0 + STRIP_W) of rows [r0, r1) of the
-// grid a describes, marched by the calling warp (warp-collective).  The
-// update's positivity flag and the Newton statistics accumulate in the
-// caller's bad and stats3 (see strip_report).
-template <bool LEARNED>
-__device__ __forceinline__ void strip_unit(const StepArgs<float>& a, int c0, int r0, int r1, float* q,
+// grid a describes, marched by the calling warp (warp-collective).  A is
+// StepArgs<float> or a view with the same members (a problem of a batch); Gp
+// is the gas in the kernel's parameter space.  The update's positivity flag
+// and the Newton statistics accumulate in the caller's bad and stats3 (see
+// strip_report).
+template <bool LEARNED, class A>
+__device__ __forceinline__ void strip_unit(const A& a, const Gas<float>* Gp, int c0, int r0, int r1, float* q,
                                            const MlpShared* M, int* stats3, unsigned& bad)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int m = a.m, n = a.n, slot = a.seq % 3;
-    const Gas<float>& G = a.G;
+    const Gas<float>& G = *Gp;
+    const StripFlushArgs fa{Gp, a.ctl, a.tau, a.htau, m, n, slot};
     const float ihx = a.pow2_x ? a.inv_hx : 1.f / a.hx, ihy = a.pow2_y ? a.inv_hy : 1.f / a.hy;
     const float ahx = a.alpha * ihx, ahy = a.alpha * ihy;
     const float hhx = a.hhx, hhy = a.hhy;
@@ -543,7 +561,7 @@ __device__ __forceinline__ void strip_unit(const StepArgs<float>& a, int c0, int
             if (vy && !qy && ky)
                 report_face(a.ctl, slot, 0, (unsigned long long)(c + 1) * (m + 1) + r, ky);
             const bool own_row = r < r1 || r == m;
-            strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, own_row, own_row, false, r, c, r, c + 1, a, M,
+            strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, own_row, own_row, false, r, c, r, c + 1, fa, M,
                                  stats3, XF0);
         }
         // prefetch the next rows (after the x-faces, while the y-faces are computed)
@@ -617,7 +635,7 @@ __device__ __forceinline__ void strip_unit(const StepArgs<float>& a, int c0, int
                     report_face(a.ctl, slot, 1, (unsigned long long)q1 * (n + 1) + cA, kx);
                 if (needB && !qy && ky)
                     report_face(a.ctl, slot, 1, (unsigned long long)q1 * (n + 1) + cB, ky);
-                strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, ownA, ownB, true, q1, cA, q1, cB, a,
+                strip_queue<LEARNED>(q, L, R, qx, qy, ux && qx, uy && qy, ownA, ownB, true, q1, cA, q1, cB, fa,
                                      M, stats3, YF);
             }
             // update of row r-1: x-faces r-1 (XFm) and r (XF0), y-faces A, B and the next lane's A
@@ -751,7 +769,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
             break;
         const int seg = u / nstrip, strip = u - seg * nstrip;
         const int r0 = seg * sa.seg;
-        strip_unit<LEARNED>(a, strip * STRIP_W, r0, (r0 + sa.seg < a.m) ? r0 + sa.seg : a.m, q, M, stats3, bad);
+        strip_unit<LEARNED>(a, &a.G, strip * STRIP_W, r0, (r0 + sa.seg < a.m) ? r0 + sa.seg : a.m, q, M, stats3, bad);
     }
     strip_report(a.ctl, a.seq % 3, a.stats, stats3, bad);
 }

@@ -470,7 +470,8 @@ class Batch:
         for k in range(lib().hydro_batch_num_shapes()):
             s = (ctypes.c_int * 4)()
             lib().hydro_batch_shape(k, s)
-            out.append({"tile_x": s[0], "tile_y": s[1], "threads": s[2], "min_ctas_per_sm": s[3]})
+            out.append({"tile_x": s[0], "tile_y": s[1], "threads": s[2], "min_ctas_per_sm": s[3],
+                        "kind": "strip" if lib().hydro_batch_shape_kind(k) == 1 else "tile"})
         return out
 
     def autotune(self, cfg, steps=3):

@@ -218,7 +218,8 @@ int hydro2d_set_mlp(hydro2d_t *h, const float *params);
  * all problems; t_all is ignored.
  * Schedules: 0/1 persistent cooperative kernel, static tiles (problem-major /
  * largest problem first), 2/3 the same with a dynamic tile counter, 4 a CUDA
- * graph of one launch per step.  The persistent kernel separates the steps
+ * graph of one launch per step.  Shapes: tiles of the one-grid tile kernel, or
+ * strip units (60 columns x a run of rows) of the one-grid strip kernel.  The persistent kernel separates the steps
  * with a grid barrier whose wait is limited (default 5 s,
  * hydro_batch_set_wait_limit); a wait that runs out makes the run return -2. */
 typedef struct hydro_batch hydro_batch_t;
@@ -239,8 +240,12 @@ int hydro_batch_download(hydro_batch_t *b, int p, double *rho, double *u, double
 int hydro_batch_run(hydro_batch_t *b, const double *cfg, int ncfg, int steps, int stats, hydro_batch_info *info);
 int hydro_batch_num_shapes(void);
 int hydro_batch_num_schedules(void);
-/* out4 = {tile cells along y, along x, threads, min CTAs per SM} */
+/* out4 = {tile cells along y, along x, threads, min CTAs per SM}; for a strip
+ * shape {columns a strip updates, rows per work unit, threads, min CTAs per SM} */
 int hydro_batch_shape(int shape, int *out4);
+/* 0: tiles (the one-grid tile kernel's code), 1: strips (the one-grid strip
+ * kernel's per-unit march; at most 576 problems). */
+int hydro_batch_shape_kind(int shape);
 int hydro_batch_set_schedule(hydro_batch_t *b, int shape, int schedule);
 int hydro_batch_set_wait_limit(hydro_batch_t *b, double seconds);
 /* Times every (shape, schedule) pair on `steps` steps of the uploaded states

@@ -56,6 +56,30 @@ def _one_problem_fp32(hg, prob, m, n, bx=-4, by=-4, steps=STEPS):
         s.close()
 
 
+def _one_problem_strip(hg, prob, m, n, rows, bx=-4, by=-4, steps=STEPS):
+    """The one-problem FP32 run with the strip kernel of `rows` rows per work
+    unit, the per-unit march the batch's strip shapes run."""
+    cfg = hg.config_2d(t_all=-1, steps=steps, hx=1.0 / m, hy=1.0 / n, bx=bx, by=by)
+    s = hg.Solver2D(m, n, hg.FORM_FP32)
+    try:
+        for k in range(s.num_variants()):
+            s.set_variant(k)
+            v = s.variant()[1]
+            if v["kernel"] == "strip" and v["tile_x"] == rows:
+                break
+        else:
+            raise AssertionError(f"no strip variant with {rows} rows per unit")
+        s.upload(*prob, None, float(cfg[6]))
+        info = s.run(cfg)
+        return s.download(), info
+    finally:
+        s.close()
+
+
+def _strip_shapes(hg):
+    return [(k, sh["tile_y"]) for k, sh in enumerate(hg.Batch.shapes()) if sh["kind"] == "strip"]
+
+
 @pytest.mark.gpu
 def test_batch_matches_one_problem_runs(gpu_lib):
     hg = gpu_lib
@@ -68,6 +92,56 @@ def test_batch_matches_one_problem_runs(gpu_lib):
         assert pinfo[k]["tau"] == winfo.tau
         for f in FIELDS + ("E",):
             assert rel_l1(got[k][f], want[f]) <= 1e-6, (k, f, rel_l1(got[k][f], want[f]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", [0, 3, 4])
+def test_batch_strip_shapes_match_one_problem_strip_runs(gpu_lib, schedule):
+    """The strip shapes run the one-grid strip kernel's per-unit march on each
+    problem: every problem equals its one-problem strip run (same rows per
+    unit) to FP32 rounding, and its time step bit for bit."""
+    hg = gpu_lib
+    probs = _problems(hg)
+    cfg = _cfg(hg, bx=-7, by=-2)
+    strips = _strip_shapes(hg)
+    assert strips
+    for sh, rows in strips:
+        got, info, pinfo = _run_batch(hg, probs, cfg, sh, schedule)
+        assert info.steps == STEPS and info.halted_problems == 0 and info.shape == sh
+        for k, (m, n) in enumerate(SIZES):
+            want, winfo = _one_problem_strip(hg, probs[k], m, n, rows, bx=-7, by=-2)
+            assert pinfo[k]["tau"] == winfo.tau
+            for f in FIELDS + ("E",):
+                assert rel_l1(got[k][f], want[f]) <= 1e-6, (sh, k, f, rel_l1(got[k][f], want[f]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("schedule", [2, 4])
+def test_batch_strip_halts_per_problem(gpu_lib, schedule):
+    """A problem whose state goes bad halts alone in a strip shape too, at the
+    step and with the state of its one-problem strip run (the step it halted
+    on is the tile shapes' too)."""
+    hg = gpu_lib
+    probs = [list(a) for a in _problems(hg)]
+    bad = 2
+    probs[bad][3] = probs[bad][3].copy()
+    probs[bad][3][10, 10] = -1.0
+    cfg = _cfg(hg)
+    sh, rows = _strip_shapes(hg)[0]
+    got, info, pinfo = _run_batch(hg, probs, cfg, shape=sh, schedule=schedule)
+    _, _, tinfo = _run_batch(hg, probs, cfg, shape=0, schedule=2)
+    assert pinfo[bad]["halted"] != 0
+    assert pinfo[bad]["halted"] == tinfo[bad]["halted"]
+    assert pinfo[bad]["halted_step"] == tinfo[bad]["halted_step"]
+    for k, (m, n) in enumerate(SIZES):
+        if k != bad:
+            assert pinfo[k]["halted"] == 0
+    want, winfo = _one_problem_strip(hg, probs[bad], *SIZES[bad], rows)
+    assert winfo.halted == pinfo[bad]["halted"]
+    for f in FIELDS:
+        ok = ~np.isnan(want[f])
+        assert np.array_equal(np.isnan(got[bad][f]), ~ok), f
+        assert rel_l1(got[bad][f][ok], want[f][ok]) <= 1e-6, f
 
 
 @pytest.mark.gpu
@@ -233,7 +307,8 @@ def test_batch_sizes_are_seeded_and_in_range():
 
 
 @pytest.mark.gpu
-def test_batch_barrier_wait_runs_out(gpu_lib):
+@pytest.mark.parametrize("kind", ["tile", "strip"])
+def test_batch_barrier_wait_runs_out(gpu_lib, kind):
     """The persistent schedule's grid barrier gives up when its wait limit runs
     out: with a limit of a nanosecond the first block to arrive stops waiting,
     every block leaves the time loop, the run returns -2 with the barrier error
@@ -243,7 +318,8 @@ def test_batch_barrier_wait_runs_out(gpu_lib):
     cfg = _cfg(hg)
     b = hg.Batch(SIZES)
     try:
-        b.set_schedule(0, 0)  # one persistent cooperative kernel for all steps
+        shape = 0 if kind == "tile" else _strip_shapes(hg)[0][0]
+        b.set_schedule(shape, 0)  # one persistent cooperative kernel for all steps
         for k, (rho, u, v, p) in enumerate(probs):
             b.upload(k, rho, u, v, p, gamma=float(cfg[6]))
         b.set_wait_limit(1e-9)
@@ -262,7 +338,7 @@ def test_batch_barrier_wait_runs_out(gpu_lib):
         got = [b.download(k) for k in range(len(SIZES))]
     finally:
         b.close()
-    ref, _, _ = _run_batch(hg, probs, cfg, 0, 0)
+    ref, _, _ = _run_batch(hg, probs, cfg, shape, 0)
     for k in range(len(SIZES)):
         for f in FIELDS:
             assert np.array_equal(got[k][f], ref[k][f])
