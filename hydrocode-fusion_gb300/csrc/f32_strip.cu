@@ -12,11 +12,18 @@ void variants_f32_strip(std::vector<StepVariant<float>>& v, bool learned)
     // the storage as L1 (for the kernel's register spills and the rows in
     // flight), or the smallest shared-memory configuration that holds two CTAs
     // (100 KB with the network image, else 64 KB) and the rest as L1
+    // (learned form: the network on queue flushes of 16 or more faces, or only
+    // on full warps of 32)
     if (learned) {
         v.push_back(strip_variant<4, 1, true>(16, 50));
         v.push_back(strip_variant<4, 1, true>(32, 50));
         v.push_back(strip_variant<4, 1, true>(16, 43));
         v.push_back(strip_variant<4, 1, true>(32, 43));
+        v.push_back(strip_variant<4, 1, true>(16, 43, 32));
+        v.push_back(strip_variant<4, 1, true>(32, 43, 32));
+        // the network image read through L1: the plain kernel's shared memory and split
+        v.push_back(strip_variant<4, 1, true>(16, 28, 32, 1));
+        v.push_back(strip_variant<4, 1, true>(16, 28, 16, 1));
     } else {
         v.push_back(strip_variant<4, 1, false>(16, 50));
         v.push_back(strip_variant<4, 1, false>(32, 50));

@@ -128,6 +128,14 @@ __device__ __forceinline__ void mlp_load_shared(MlpShared& S, const uint32_t* __
         S.b3 = prm[MLP_B3];
 }
 
+// The shared-memory image of the network built once in global memory, for
+// kernels that read it through L1 instead of staging it (one block).
+static __global__ void k_mlp_image(const uint32_t* __restrict__ frag, const float* __restrict__ prm,
+                                   MlpShared* __restrict__ img)
+{
+    mlp_load_shared(*img, frag, prm, threadIdx.x, blockDim.x);
+}
+
 __device__ __forceinline__ float relu(float v) { return v > 0.f ? v : 0.f; }
 
 // Warp-cooperative forward pass: all 32 lanes call it with their own features

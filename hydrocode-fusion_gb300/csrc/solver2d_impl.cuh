@@ -43,6 +43,8 @@ struct StepVariant {
     StepMaps maps[2];  // tma: descriptors of the two state buffers
     int strip = 0;
     int carve = 100;   // shared-memory carve-out of the L1/shared storage, per cent
+    int mlp_min = STRIP_MLP_MIN;  // strip kernel, learned form: smallest flush the network runs on
+    int mlp_global = 0;           // strip kernel, learned form: network image read from global memory
 };
 
 template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int RS = 0>
@@ -61,12 +63,16 @@ StepVariant<R> tma_variant()
 }
 
 template <int NW, int MINB, bool LEARNED>
-StepVariant<float> strip_variant(int seg, int carve)
+StepVariant<float> strip_variant(int seg, int carve, int mlp_min = STRIP_MLP_MIN, int mlp_global = 0)
 {
-    StepVariant<float> v{seg, STRIP_W, NW * 32, MINB, StripSmem<NW, LEARNED>::bytes,
+    // a learned variant that reads the network image from global memory needs no shared copy of it
+    StepVariant<float> v{seg, STRIP_W, NW * 32, MINB,
+                         (LEARNED && !mlp_global) ? StripSmem<NW, true>::bytes : StripSmem<NW, false>::bytes,
                          (const void*)k_step_strip<NW, MINB, LEARNED>, 0, 0, {}};
     v.strip = 1;
     v.carve = carve;
+    v.mlp_min = mlp_min;
+    v.mlp_global = mlp_global;
     return v;
 }
 
@@ -394,7 +400,8 @@ public:
         variants = TS::all(form == HYDRO_FORM_FP32_LEARNED, rs);
         if (form == HYDRO_FORM_FP32_LEARNED) {
             if (!cuda_ok(cudaMalloc(&mlp_frag, sizeof(uint32_t) * MLP_NFRAG), "network") ||
-                !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network"))
+                !cuda_ok(cudaMalloc(&mlp_prm, sizeof(float) * MLP_NPARAM), "network") ||
+                !cuda_ok(cudaMalloc(&mlp_img, sizeof(MlpShared)), "network"))
                 return -1;
         }
         int smem_optin = 0;
@@ -405,7 +412,12 @@ public:
                 v.occ = 0;
                 continue;
             }
-            if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem),
+            // variants of one kernel may differ in their shared memory: allow the largest
+            size_t smax = v.smem;
+            for (const auto& w : variants)
+                if (w.kern == v.kern && (int)w.smem <= smem_optin && w.smem > smax)
+                    smax = w.smem;
+            if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax),
                          "smem attr"))
                 return -1;
             // the unified L1/shared storage: all of it as shared memory (several tile CTAs fit
@@ -467,6 +479,7 @@ public:
 
     uint32_t* mlp_frag = nullptr;
     float* mlp_prm = nullptr;
+    MlpShared* mlp_img = nullptr;  // the shared-memory image in global memory
     bool mlp_set = false;
 
     int set_mlp(const float* params) override
@@ -479,7 +492,8 @@ public:
                      "network upload"))
             return -1;
         k_mlp_pack<<<(8 * 32 + 4 * 8 * 32 + 4 * 32 + 127) / 128, 128, 0, stream>>>(mlp_prm, mlp_frag);
-        count_launch(1);
+        k_mlp_image<<<1, 256, 0, stream>>>(mlp_frag, mlp_prm, mlp_img);
+        count_launch(2);
         mlp_set = true;
         return cuda_ok(cudaStreamSynchronize(stream), "network pack") ? 0 : -1;
     }
@@ -489,6 +503,7 @@ public:
         if (stream) cudaStreamSynchronize(stream);
         cudaFree(mlp_frag);
         cudaFree(mlp_prm);
+        cudaFree(mlp_img);
         cudaFree(mem);
         cudaFree(ghost0);
         cudaFree(ctl);
@@ -786,8 +801,12 @@ public:
             cur_w = w0;
             hydro_run_info info;
             int nt;
-            // a variant that fails to run is timed as infinitely slow
-            float ms = run(r2, 0, 0, tp, 2, 2, nullptr, &info, &nt) ? 3e38f : (float)info.gpu_ms;
+            // a variant that fails to run is timed as infinitely slow (and its launch error is
+            // cleared, so that it is not reported by the next variant's run)
+            const bool failed = run(r2, 0, 0, tp, 2, 2, nullptr, &info, &nt) != 0;
+            if (failed)
+                cudaGetLastError();
+            float ms = failed ? 3e38f : (float)info.gpu_ms;
             if (times_ms)
                 times_ms[v] = ms;
             if (ms < best_ms) {
@@ -850,6 +869,7 @@ public:
             }
             a.mlp_frag = mlp_frag;
             a.mlp_prm = mlp_prm;
+            a.mlp_img = mlp_img;
         }
 
         using TS = Variants<R>;
@@ -903,6 +923,8 @@ public:
                     StripArgs sa;
                     sa.work = work;
                     sa.seg = V.TJ;
+                    sa.mlp_min = V.mlp_min;
+                    sa.mlp_global = V.mlp_global;
                     void* args[] = {(void*)&a, (void*)&sa};
                     // variants of one kernel differ in their L1/shared split: set per launch
                     cudaLaunchConfig_t lc;

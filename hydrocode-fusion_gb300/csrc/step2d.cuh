@@ -77,6 +77,7 @@ struct StepArgs {
     int stats;             // count Newton faces / iterations
     const uint32_t* mlp_frag;  // learned form: packed BF16 network
     const float* mlp_prm;      // learned form: FP32 parameters (biases)
+    const void* mlp_img;       // learned form: the network's shared-memory image (MlpShared) in global memory
 };
 
 // ---------------------------------------------------------------------------

@@ -36,9 +36,10 @@ namespace hydro {
 constexpr int STRIP_W = 60;      // columns a strip updates (64 loaded)
 constexpr int STRIP_QCAP = 64;   // queued faces per warp per flush
 constexpr int STRIP_QWORDS = 28; // words per queue entry
-// The learned form runs the network on a flush of at least this many faces:
-// one warp pass of the network costs about as much as the Newton iterations
-// it saves on a full warp of faces, so on a handful it would only add time.
+// The learned form runs the network on a flush of at least this many faces
+// (the default; a launch argument): one warp pass of the network costs about
+// as much as the Newton iterations it saves on a full warp of faces, so on a
+// handful it would only add time.
 constexpr int STRIP_MLP_MIN = 16;
 
 // ---------------------------------------------------------------------------
@@ -335,6 +336,7 @@ struct StripFlushArgs {
     Ctl* ctl;
     float tau, htau;
     int m, n, slot;
+    int mlp_min;  // learned form: the network runs on flushes of at least this many faces
 };
 
 template <bool LEARNED>
@@ -361,7 +363,7 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StripFl
         const bool ydir = fl & 1, retry = (fl >> 1) & 1, counted = (fl >> 2) & 1;
         float p_start = -1.f;
         if constexpr (LEARNED) {
-            if (cnt - base >= STRIP_MLP_MIN)  // warp-uniform
+            if (cnt - base >= fa.mlp_min)  // warp-uniform
                 p_start = learned_guess(L, Rr, act && !retry, G, *M, cnt - base < 32 ? cnt - base : 32);
         }
         if (!act)
@@ -460,6 +462,8 @@ __device__ __forceinline__ void strip_queue(float* q, const SSide2& L, const SSi
 struct StripArgs {
     unsigned int* work;  // three rotating per-launch unit counters
     int seg;             // rows per work unit
+    int mlp_min;         // learned form: smallest queue flush the network runs on
+    int mlp_global;      // learned form: 1 = read the network image from global memory (through L1)
 };
 
 template <int NW, bool LEARNED>
@@ -477,13 +481,13 @@ struct StripSmem {
 // strip_report).
 template <bool LEARNED, class A>
 __device__ __forceinline__ void strip_unit(const A& a, const Gas<float>* Gp, int c0, int r0, int r1, float* q,
-                                           const MlpShared* M, int* stats3, unsigned& bad)
+                                           const MlpShared* M, int mlp_min, int* stats3, unsigned& bad)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int m = a.m, n = a.n, slot = a.seq % 3;
     const Gas<float>& G = *Gp;
-    const StripFlushArgs fa{Gp, a.ctl, a.tau, a.htau, m, n, slot};
+    const StripFlushArgs fa{Gp, a.ctl, a.tau, a.htau, m, n, slot, mlp_min};
     const float ihx = a.pow2_x ? a.inv_hx : 1.f / a.hx, ihy = a.pow2_y ? a.inv_hy : 1.f / a.hy;
     const float ahx = a.alpha * ihx, ahy = a.alpha * ihy;
     const float hhx = a.hhx, hhy = a.hhy;
@@ -749,9 +753,13 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
     float* q = reinterpret_cast<float*>(smem_raw + warp * SM::q_bytes);
     const MlpShared* M = reinterpret_cast<const MlpShared*>(smem_raw + SM::mlp_off);
     if (LEARNED) {
-        mlp_load_shared(*reinterpret_cast<MlpShared*>(smem_raw + SM::mlp_off), a.mlp_frag, a.mlp_prm, threadIdx.x,
-                        NW * 32);
-        __syncthreads();
+        if (sa.mlp_global) {  // (block-uniform) no shared-memory image: the launch did not allocate one
+            M = reinterpret_cast<const MlpShared*>(a.mlp_img);
+        } else {
+            mlp_load_shared(*reinterpret_cast<MlpShared*>(smem_raw + SM::mlp_off), a.mlp_frag, a.mlp_prm,
+                            threadIdx.x, NW * 32);
+            __syncthreads();
+        }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0)
         sa.work[(a.seq + 1) % 3] = 0u;  // the next launch's counter (this launch's was cleared by the previous one)
@@ -769,7 +777,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
             break;
         const int seg = u / nstrip, strip = u - seg * nstrip;
         const int r0 = seg * sa.seg;
-        strip_unit<LEARNED>(a, &a.G, strip * STRIP_W, r0, (r0 + sa.seg < a.m) ? r0 + sa.seg : a.m, q, M, stats3, bad);
+        strip_unit<LEARNED>(a, &a.G, strip * STRIP_W, r0, (r0 + sa.seg < a.m) ? r0 + sa.seg : a.m, q, M, sa.mlp_min,
+                            stats3, bad);
     }
     strip_report(a.ctl, a.seq % 3, a.stats, stats3, bad);
 }
