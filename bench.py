@@ -514,6 +514,7 @@ def main():
     ap.add_argument("--no-shear", action="store_true")
     ap.add_argument("--no-g2d", action="store_true")
     ap.add_argument("--no-mf", action="store_true")
+    ap.add_argument("--no-costs", action="store_true", help="skip the learned start's per-face cost parts")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=300)
     args = ap.parse_args()
@@ -616,6 +617,16 @@ def main():
                "speedup_over_plain_fp32": plain["ms_per_step"] / head["ms_per_step"],
                "speedup_over_fp64": forms["speedup_learned_over_fp64"],
                "newton_learned": head.get("newton"), "newton_plain": plain.get("newton")}
+    # the learned start's parts per face, in the FP32 form's code (1 M seeded exact-path faces)
+    if rank == 0 and not args.no_costs:
+        try:
+            c = hg.learned_costs(nfaces=1 << 20)
+            c["faces"] = "1048576 seeded pairs, four-quadrant ranges, all through the exact path"
+            c["network_vs_iteration"] = (c["network_ns_per_face"] / c["ns_per_newton_iteration"]
+                                         if c["ns_per_newton_iteration"] > 0 else None)
+            learned["costs"] = c
+        except Exception as exc:  # reported, not fatal: the timed forms above are the headline
+            learned["costs"] = {"error": str(exc)}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",

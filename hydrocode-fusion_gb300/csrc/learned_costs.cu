@@ -1,0 +1,182 @@
+// learned_costs.cu -- what the learned Newton start costs and saves, per face,
+// in the FP32 form's own device code (no reference counterpart).
+//
+// Seeded Riemann pairs with the four-quadrant data's ranges (rho, p in
+// [0.1, 2], u, v in [-1, 1], slopes in [-1, 1]), all sent through the exact
+// path (the acoustic shortcut is skipped), one thread per face, full warps:
+//   * the network: features and the three BF16 MMA layers (warp_mlp_outline);
+//   * the exact Riemann solve (q1d_star_exact, the Newton iteration with the
+//     FP64 fallback) from the reference's start and from the network's start,
+//     with the iterations each needs: their difference over the iterations
+//     saved is the cost of one FP32 Newton iteration;
+//   * the nonlinear GRP derivatives and fluxes after the solve (q1d_waves,
+//     q1d_derivs), as the time of solve + derivatives less the solve.
+// Each kernel is timed with CUDA events over all faces, after one untimed run.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include "solver2d_impl.cuh"
+
+namespace hydro {
+
+__device__ __forceinline__ float cost_uniform(unsigned long long& s, float lo, float hi)
+{
+    s += 0x9e3779b97f4a7c15ull;
+    unsigned long long z = s;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    return lo + (hi - lo) * (float)(z >> 40) * (1.0f / 16777216.0f);
+}
+
+__device__ __forceinline__ void cost_face(int i, unsigned long long seed, Side<float>& L, Side<float>& R)
+{
+    unsigned long long s = seed ^ (0x632be59bd9b4e019ull * (unsigned long long)(i + 1));
+    L.rho = cost_uniform(s, 0.1f, 2.f); L.u = cost_uniform(s, -1.f, 1.f); L.v = cost_uniform(s, -1.f, 1.f);
+    L.p = cost_uniform(s, 0.1f, 2.f);
+    R.rho = cost_uniform(s, 0.1f, 2.f); R.u = cost_uniform(s, -1.f, 1.f); R.v = cost_uniform(s, -1.f, 1.f);
+    R.p = cost_uniform(s, 0.1f, 2.f);
+    L.drho = cost_uniform(s, -1.f, 1.f); L.du = cost_uniform(s, -1.f, 1.f); L.dv = cost_uniform(s, -1.f, 1.f);
+    L.dp = cost_uniform(s, -1.f, 1.f);
+    R.drho = cost_uniform(s, -1.f, 1.f); R.du = cost_uniform(s, -1.f, 1.f); R.dv = cost_uniform(s, -1.f, 1.f);
+    R.dp = cost_uniform(s, -1.f, 1.f);
+    L.trho = L.tu = L.tv = L.tp = 0.f;
+    R.trho = R.tu = R.tv = R.tp = 0.f;
+}
+
+// the network's starting pressure of every face
+__global__ void __launch_bounds__(256) k_cost_mlp(int n, unsigned long long seed, Gas<float> G,
+                                                  const MlpShared* __restrict__ img, float* __restrict__ p_start)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    Side<float> L, R;
+    cost_face(i, seed, L, R);
+    const float cL = sqrtf(G.g * L.p / L.rho), cR = sqrtf(G.g * R.p / R.rho);
+    float x[6];
+    const float pbar = mlp_features(L.rho, L.u, L.p, cL, R.rho, R.u, R.p, cR, x);
+    const float y = warp_mlp_outline(x[0], x[1], x[2], x[3], x[4], x[5], img, 32);
+    if (i < n)
+        p_start[i] = pbar * __expf(y);
+}
+
+// the exact solve (DERIVS: and the nonlinear GRP derivatives and fluxes)
+template <bool DERIVS>
+__global__ void __launch_bounds__(256) k_cost_solve(int n, unsigned long long seed, Gas<float> G, float tau,
+                                                    const float* __restrict__ p_start, int* __restrict__ iters,
+                                                    float* __restrict__ sink)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    Side<float> L, R;
+    cost_face(i, seed, L, R);
+    Star<float> S;
+    S.c_L = sqrtf(G.g * L.p / L.rho);
+    S.c_R = sqrtf(G.g * R.p / R.rho);
+    S.acoustic = 0;
+    StarInfo st;
+    st.fallback = 0;
+    q1d_star_exact<float>(L, R, G, S, st, p_start ? p_start[i] : -1.f);
+    float out = S.p_star + S.u_star;
+    if constexpr (DERIVS) {
+        q1d_waves(L, R, G, S);
+        float D[4], U[4];
+        q1d_derivs<float, 2>(L, R, G, S, D, U);
+        FaceOut<float> o;
+        face_flux<float>(D, U, tau, 0.5f * tau, G, o, false);
+        out += o.F[0] + o.F[1] + o.F[2] + o.F[3] + o.I[0] + o.I[1] + o.I[2] + o.I[3];
+    }
+    iters[i] = st.iters;
+    sink[i] = out;  // keeps the work
+}
+
+}  // namespace hydro
+
+using namespace hydro;
+
+extern "C" int hydro_learned_costs(const float* params, int nfaces, unsigned long long seed, double gamma,
+                                   double* out)
+{
+    memset(out, 0, sizeof(double) * 8);
+    if (nfaces < 32 || !params) {
+        set_error("learned_costs: at least 32 faces and the network's parameters");
+        return -1;
+    }
+    const int n = nfaces / 32 * 32;
+    float *prm = nullptr, *p_start = nullptr, *sink = nullptr;
+    uint32_t* frag = nullptr;
+    MlpShared* img = nullptr;
+    int* iters = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = -1;
+    std::vector<int> it(n);
+    float ms[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    double mean_it[2] = {0.0, 0.0};
+    Gas<float> G;
+    fill_gas_params(G, gamma, 1e-9);
+    const dim3 grid((n + 255) / 256), block(256);
+    if (!cuda_ok(cudaMalloc(&prm, sizeof(float) * MLP_NPARAM), "costs") ||
+        !cuda_ok(cudaMalloc(&frag, sizeof(uint32_t) * MLP_NFRAG), "costs") ||
+        !cuda_ok(cudaMalloc(&img, sizeof(MlpShared)), "costs") ||
+        !cuda_ok(cudaMalloc(&p_start, sizeof(float) * n), "costs") ||
+        !cuda_ok(cudaMalloc(&sink, sizeof(float) * n), "costs") ||
+        !cuda_ok(cudaMalloc(&iters, sizeof(int) * n), "costs") || !cuda_ok(cudaEventCreate(&e0), "event") ||
+        !cuda_ok(cudaEventCreate(&e1), "event"))
+        goto done;
+    if (!cuda_ok(cudaMemcpy(prm, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice), "costs"))
+        goto done;
+    k_mlp_pack<<<(8 * 32 + 4 * 8 * 32 + 4 * 32 + 127) / 128, 128>>>(prm, frag);
+    k_mlp_image<<<1, 256>>>(frag, prm, img);
+    count_launch(2);
+    // each kernel: one untimed run, then one timed
+    for (int k = 0; k < 5; ++k) {
+        for (int rep = 0; rep < 2; ++rep) {
+            if (rep)
+                cudaEventRecord(e0);
+            switch (k) {
+            case 0: k_cost_mlp<<<grid, block>>>(n, seed, G, img, p_start); break;
+            case 1: k_cost_solve<false><<<grid, block>>>(n, seed, G, 1e-4f, nullptr, iters, sink); break;
+            case 2: k_cost_solve<false><<<grid, block>>>(n, seed, G, 1e-4f, p_start, iters, sink); break;
+            case 3: k_cost_solve<true><<<grid, block>>>(n, seed, G, 1e-4f, nullptr, iters, sink); break;
+            default: k_cost_solve<true><<<grid, block>>>(n, seed, G, 1e-4f, p_start, iters, sink); break;
+            }
+            count_launch();
+            if (rep)
+                cudaEventRecord(e1);
+        }
+        if (!cuda_ok(cudaEventSynchronize(e1), "costs run"))
+            goto done;
+        cudaEventElapsedTime(&ms[k], e0, e1);
+        if (k == 1 || k == 2) {
+            if (!cuda_ok(cudaMemcpy(it.data(), iters, sizeof(int) * n, cudaMemcpyDeviceToHost), "costs"))
+                goto done;
+            double s = 0.0;
+            for (int v : it)
+                s += v;
+            mean_it[k - 1] = s / n;
+        }
+    }
+    {
+        const double per = 1e6 / n;  // ms -> ns per face
+        out[0] = ms[0] * per;                             // network, per face
+        out[1] = ms[1] * per;                             // exact solve, reference start
+        out[2] = mean_it[0];                              // its Newton iterations per face
+        out[3] = ms[2] * per;                             // exact solve, network start (network not included)
+        out[4] = mean_it[1];                              // its Newton iterations per face
+        out[5] = (mean_it[0] - mean_it[1]) > 0.0 ? (out[1] - out[3]) / (mean_it[0] - mean_it[1]) : 0.0;
+        out[6] = (ms[3] - ms[1]) * per;                   // GRP derivatives and fluxes after the solve
+        out[7] = ms[3] * per;                             // the whole exact face, reference start
+        rc = 0;
+    }
+done:
+    cudaFree(prm);
+    cudaFree(frag);
+    cudaFree(img);
+    cudaFree(p_start);
+    cudaFree(sink);
+    cudaFree(iters);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return rc;
+}

@@ -412,6 +412,27 @@ def fp64_peak() -> float:
     return float(v.value)
 
 
+LEARNED_COST_KEYS = ("network_ns_per_face", "solve_ns_per_face_reference_start", "iters_reference_start",
+                     "solve_ns_per_face_learned_start", "iters_learned_start", "ns_per_newton_iteration",
+                     "grp_derivatives_ns_per_face", "exact_face_ns_per_face")
+
+
+def learned_costs(params=None, nfaces: int = 1 << 20, seed: int = 7, gamma: float = 1.4) -> dict:
+    """What the learned start costs and saves per face in the FP32 form's device
+    code (hydro_learned_costs): the network pass, the exact solve from either
+    start with its iterations, one Newton iteration, the GRP derivatives."""
+    prm = np.ascontiguousarray(load_weights() if params is None else params, np.float32)
+    out = (ctypes.c_double * 8)()
+    L = lib()
+    L.hydro_learned_costs.restype = ctypes.c_int
+    L.hydro_learned_costs.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_ulonglong,
+                                      ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    if L.hydro_learned_costs(prm.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), int(nfaces), int(seed),
+                             float(gamma), out) != 0:
+        raise RuntimeError("hydro_learned_costs failed: " + last_error())
+    return dict(zip(LEARNED_COST_KEYS, (float(v) for v in out)))
+
+
 def load_weights(path: str = WEIGHTS_PATH) -> np.ndarray:
     w = np.fromfile(path, dtype="<f4")
     if w.size != MLP_NPARAM:

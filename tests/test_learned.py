@@ -100,3 +100,20 @@ def test_learned_guess_saves_newton_iterations(gpu_lib):
         rel_plain = np.abs(plain[f] - ref[f]).sum() / np.abs(ref[f]).sum()
         bound = 1.25 * rel_plain + 1e-7 if f == "v" else 1e-5
         assert rel <= bound, (f, rel, rel_plain)
+
+
+@pytest.mark.gpu
+def test_learned_start_cost_parts(gpu_lib):
+    """hydro_learned_costs on 64 K seeded exact-path faces with the shipped
+    weights: every part takes time, the network's start needs fewer Newton
+    iterations than the reference's, and the per-iteration cost it derives is
+    positive (the parts the learned-start analysis is built on)."""
+    hg = gpu_lib
+    c = hg.learned_costs(nfaces=65536, seed=3)
+    for k in ("network_ns_per_face", "solve_ns_per_face_reference_start", "solve_ns_per_face_learned_start",
+              "grp_derivatives_ns_per_face", "exact_face_ns_per_face"):
+        assert c[k] > 0, (k, c)
+    assert 1.0 <= c["iters_learned_start"] < c["iters_reference_start"], c
+    assert c["ns_per_newton_iteration"] > 0, c
+    with pytest.raises(RuntimeError):
+        hg.learned_costs(nfaces=16)
