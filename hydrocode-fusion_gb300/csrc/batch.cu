@@ -1010,6 +1010,15 @@ int hydro_batch_autotune(hydro_batch* b, const double* cfg, int ncfg, int steps,
     const int nshape = (int)batch_shapes().size();
     for (int sh = 0; sh < nshape; ++sh)
         for (int sc = 0; sc < BATCH_SCHEDULES; ++sc) {
+            // The strip shapes are not candidates: timed over the first steps of a run they come
+            // within ~20% of the tiles, but their warps solve the exact faces of a discontinuity
+            // along the march one or two at a time, and as a run develops more of those faces they
+            // fall far behind (5 against 8.6 G cell-updates/s over 300 steps of 512 problems).
+            if (batch_shapes()[sh].strip) {
+                if (times_ms)
+                    times_ms[sh * BATCH_SCHEDULES + sc] = 3e38f;
+                continue;
+            }
             cudaMemcpyAsync(b->mem, backup, sizeof(float) * total, cudaMemcpyDeviceToDevice, b->stream);
             b->shape = sh;
             b->schedule = sc;

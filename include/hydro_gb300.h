@@ -260,7 +260,9 @@ int hydro_batch_set_schedule(hydro_batch_t *b, int shape, int schedule);
 int hydro_batch_set_wait_limit(hydro_batch_t *b, double seconds);
 /* Times every (shape, schedule) pair on `steps` steps of the uploaded states
  * (restored afterwards), keeps the fastest and returns shape * schedules +
- * schedule; times_ms (may be NULL) receives shapes x schedules values. */
+ * schedule; times_ms (may be NULL) receives shapes x schedules values.  The
+ * strip shapes are not timed (3e38): their first steps do not predict a long
+ * run; hydro_batch_set_schedule selects them. */
 int hydro_batch_autotune(hydro_batch_t *b, const double *cfg, int ncfg, int steps, float *times_ms);
 /* Outcome of problem p in the last run: halted (0 no, 1 abort, 2 stop), the
  * step it halted on, and its time step. */
