@@ -15,6 +15,8 @@ CASES = [
     (70, 45, -4, -4, 3),
     (45, 70, -7, -2, 5),
     (33, 96, -24, -1, 8),
+    # strips and row units with interior ones on both axes (the strip kernel's fast path)
+    (150, 200, -4, -7, 9),
 ]
 STEPS = 12
 
