@@ -50,6 +50,7 @@ class Call2D:
         self.time_plot[-1] = cfg[1]
         if ntp:
             self.time_plot[1:-1] = plot_times
+        self._time_plot0 = self.time_plot.copy()
         self.data = np.zeros((self.N_T, 5, m, n))
         d0 = self.data[0]
         d0[0], d0[1], d0[2], d0[3] = rho, u, v, p
@@ -64,8 +65,11 @@ class Call2D:
         self.cpu_time = np.zeros(self.N_T)
 
     def call(self):
+        """Runs the scheme from the initial data in CV[0]; repeatable (the plot
+        times, which the call overwrites with the times reached, are reset)."""
         conf = config_view(self.lib)
         conf[:] = self.cfg
+        self.time_plot[:] = self._time_plot0
         nplot = ctypes.c_int(self.N_plot0)
         fn = self.lib.GRP_solver_2D_split_EUL_source if self.split else self.lib.GRP_solver_2D_EUL_source
         fn.restype = None
