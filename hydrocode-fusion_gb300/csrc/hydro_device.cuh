@@ -215,7 +215,34 @@ struct Gas {
     R op2z;   // 1 + 2 zeta
     R eps;
     double g64, eps64;  // FP64 copies for the FP32 form's FP64 Newton fallback
+    double dist2_max;   // FP64 uniform-pair test: sqrt(d2) < eps exactly when d2 <= dist2_max
 };
+
+// The largest double d2 whose correctly rounded square root is below eps, or -1
+// when there is none (eps <= 0 or NaN).  The rounded square root is
+// non-decreasing in its argument, so for every double d2 >= 0, NaN and +inf
+// included, sqrt(d2) < eps holds exactly when d2 <= dist2_max: the FP64 form's
+// uniform-pair test makes the reference's decision without the square root.
+// eps * eps lies within a few units in the last place of the limit; each walk
+// below takes a few steps (bounded all the same).
+__host__ __device__ inline double uniform_dist2_max(double eps)
+{
+    if (!(eps > 0.0))
+        return -1.0;
+    const double big = 1.7976931348623157e308;  // the largest finite double
+    double x = eps * eps;
+    if (!(x <= big))
+        x = big;
+    for (int k = 0; k < 4096 && !(sqrt(x) < eps); ++k)  // down into the set (sqrt(0) = 0 < eps)
+        x = nextafter(x, 0.0);
+    for (int k = 0; k < 4096; ++k) {  // up to its last element
+        const double y = nextafter(x, 2.0 * big);
+        if (!(y <= big) || !(sqrt(y) < eps))
+            break;
+        x = y;
+    }
+    return x;
+}
 
 // The constants of a Gas, derived in FP64 (host for the kernels' arguments;
 // device for the FP32 form's FP64 retry of a face).
@@ -239,6 +266,7 @@ __host__ __device__ inline void gas_fill(Gas<R>& G, double g, double eps)
     G.eps = (R)eps;
     G.g64 = g;
     G.eps64 = eps;
+    G.dist2_max = uniform_dist2_max(eps);
 }
 
 // Velocity on the 1-wave curve through (uL,pL) at pressure pp (shock for pp > pL,
@@ -649,14 +677,22 @@ __device__ __noinline__ void q1d_star_exact(const Side<R>& L, const Side<R>& Rr,
 // uniform pairs (dist < eps) take the averaged state, all others the exact solver.
 // The uniform-pair test of q1d_star (the acoustic case), on its own: used to
 // sort faces before solving them; q1d_star makes the decision again itself.
-// RS selects the interface solver: 0 = quasi-1D (linear_grp_solver_Edir_Q1D.c:92),
+// RS selects the interface solver: 0 = quasi-1D (linear_grp_solver_Edir_Q1D.c:95-96),
 // 1 = genuinely 2D, whose distance also counts the tangential velocity jump
 // (linear_grp_solver_Edir_G2D.c:112).
 template <typename R, int RS = 0>
 __device__ __forceinline__ bool face_uniform(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G)
 {
     const R rho_L = L.rho, rho_R = Rr.rho, u_L = L.u, u_R = Rr.u, p_L = L.p, p_R = Rr.p;
-    if constexpr (RS == 1) {
+    if constexpr (sizeof(R) == 8) {
+        // dist = sqrt(d2) < eps, decided on d2 itself (uniform_dist2_max): the
+        // same decision as the reference's, without an IEEE square root per face
+        R d2 = (rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R);
+        if constexpr (RS == 1)
+            d2 = d2 + (L.v - Rr.v) * (L.v - Rr.v);
+        d2 = d2 + (p_L - p_R) * (p_L - p_R);
+        return d2 <= G.dist2_max;
+    } else if constexpr (RS == 1) {
         const R v_L = L.v, v_R = Rr.v;
         R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) +
                              (v_L - v_R) * (v_L - v_R) + (p_L - p_R) * (p_L - p_R));

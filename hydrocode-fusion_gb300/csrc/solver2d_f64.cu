@@ -17,3 +17,6 @@ Solver2DBase* make_solver2d_f64(int m, int n, int rs)
 }
 
 }  // namespace hydro
+
+// The FP64 form's uniform-pair threshold (the host side of the kernels' test).
+extern "C" double hydro_uniform_dist2_max(double eps) { return hydro::uniform_dist2_max(eps); }

@@ -316,6 +316,13 @@ typedef struct {
 int hydro_grp2d_flux_mf(int nface, const double *in, double *out, int *status, const double *cfg, int ncfg,
                         double tau, hydro_face_info *info);
 
+/* The FP64 form's uniform-pair threshold (host arithmetic, no GPU): the largest
+   d2 whose correctly rounded square root is below eps (-1 if none), so that the
+   reference's test sqrt(d2) < eps (linear_grp_solver_Edir_Q1D.c:95-96,139,
+   linear_grp_solver_Edir_G2D.c:112-113,156, with atc = eps) is decided as
+   d2 <= this value. */
+double hydro_uniform_dist2_max(double eps);
+
 /* Number of CUDA kernels launched by this library since load (all solvers). */
 unsigned long long hydro_gb300_kernel_launches(void);
 /* Message of the last failing call in this thread ("" if none). */
