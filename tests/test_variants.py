@@ -51,9 +51,15 @@ def test_fp64_variants_match_oracle(gpu_lib, port, m, n, bx, by, seed):
     rho, u, v, p = cases.four_quadrant(m, n, seed)
     cfg = _cfg(hg, m, n, bx, by)
     want = port.run_2d(rho, u, v, p, cfg)
-    for shape, got in _all_variants(hg, hg.FORM_FP64, rho, u, v, p, cfg):
+    runs = _all_variants(hg, hg.FORM_FP64, rho, u, v, p, cfg)
+    for shape, got in runs:
         for f in FIELDS + ("E",):
             assert rel_l1(got[f], want[f]) <= 1e-12, (shape, f, rel_l1(got[f], want[f]))
+    # every FP64 variant computes each face, slope and cell with the same code
+    # from the same inputs: the same bits, whatever the tiling or the march
+    for shape, got in runs[1:]:
+        for f in FIELDS + ("E",):
+            assert np.array_equal(got[f], runs[0][1][f]), (shape, f)
 
 
 @pytest.mark.gpu
