@@ -407,7 +407,12 @@ public:
         int smem_optin = 0;
         cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         for (auto& v : variants) {
-            if ((int)v.smem > smem_optin) {  // too large for this device: dropped below
+            // the dynamic shared memory a CTA may have next to the kernel's static variables
+            cudaFuncAttributes fa;
+            if (!cuda_ok(cudaFuncGetAttributes(&fa, v.kern), "kernel attributes"))
+                return -1;
+            const int avail = smem_optin - (int)fa.sharedSizeBytes;
+            if ((int)v.smem > avail) {  // too large for this device: dropped below
                 v.tma = 1;
                 v.occ = 0;
                 continue;
@@ -415,7 +420,7 @@ public:
             // variants of one kernel may differ in their shared memory: allow the largest
             size_t smax = v.smem;
             for (const auto& w : variants)
-                if (w.kern == v.kern && (int)w.smem <= smem_optin && w.smem > smax)
+                if (w.kern == v.kern && (int)w.smem <= avail && w.smem > smax)
                     smax = w.smem;
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax),
                          "smem attr"))
