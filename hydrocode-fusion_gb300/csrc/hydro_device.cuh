@@ -216,6 +216,7 @@ struct Gas {
     R eps;
     double g64, eps64;  // FP64 copies for the FP32 form's FP64 Newton fallback
     double dist2_max;   // FP64 uniform-pair test: sqrt(d2) < eps exactly when d2 <= dist2_max
+                        // (set on the host; a device-side gas_fill leaves -1, no pair uniform)
 };
 
 // The largest double d2 whose correctly rounded square root is below eps, or -1
@@ -266,7 +267,11 @@ __host__ __device__ inline void gas_fill(Gas<R>& G, double g, double eps)
     G.eps = (R)eps;
     G.g64 = g;
     G.eps64 = eps;
+#ifdef __CUDA_ARCH__
+    G.dist2_max = -1.0;  // the caller passes the host's value where the test runs
+#else
     G.dist2_max = uniform_dist2_max(eps);
+#endif
 }
 
 // Velocity on the 1-wave curve through (uL,pL) at pressure pp (shock for pp > pL,

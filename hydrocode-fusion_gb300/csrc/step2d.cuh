@@ -220,10 +220,12 @@ __device__ __forceinline__ void report_face(Ctl* ctl, int slot, int dir, unsigne
 // the face passes: it runs on a handful of faces per run.
 template <int RS>
 static __device__ __noinline__ int solve_face_fp64_retry(const Side<float>& L, const Side<float>& Rr, double g,
-                                                         double eps, double tau, bool ydir, FaceOut<float>& o)
+                                                         double eps, double dist2_max, double tau, bool ydir,
+                                                         FaceOut<float>& o)
 {
     Gas<double> G;
     gas_fill(G, g, eps);
+    G.dist2_max = dist2_max;
     Side<double> Ld, Rd;
     Ld.rho = L.rho; Ld.u = L.u; Ld.v = L.v; Ld.p = L.p;
     Ld.drho = L.drho; Ld.du = L.du; Ld.dv = L.dv; Ld.dp = L.dp;
@@ -666,7 +668,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                 sides(f, L, Rr, lj, li, j, i);
                 FaceOut<R> o;
                 const bool ydir = f >= NFX;
-                const int code = solve_face_fp64_retry<RS>(L, Rr, G.g64, G.eps64, (double)a.tau, ydir, o);
+                const int code = solve_face_fp64_retry<RS>(L, Rr, G.g64, G.eps64, G.dist2_max, (double)a.tau, ydir, o);
                 if (!ydir) {
                     report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
 #pragma unroll

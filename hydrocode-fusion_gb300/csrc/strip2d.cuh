@@ -382,7 +382,7 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StripFl
             code = 2;
         }
         if (code == 2)
-            code = solve_face_fp64_retry<0>(L, Rr, G.g64, G.eps64, (double)fa.tau, ydir, o);
+            code = solve_face_fp64_retry<0>(L, Rr, G.g64, G.eps64, G.dist2_max, (double)fa.tau, ydir, o);
         if (!ydir)
             report_face(fa.ctl, slot, 0, (unsigned long long)col * (fa.m + 1) + row, code);
         else
