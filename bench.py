@@ -321,7 +321,8 @@ def e2e_run(hg, state, m, n, K):
             "call": "GRP_solver_2D_EUL_source, config[300]=2, host x-major row arrays (CV[0] in, CV[1] out)"}
 
 
-def batch_run(hg, count, steps, tune_steps, l1_sample):
+def batch_run(hg, count, steps, tune_steps, l1_sample, fixed=None):
+    """fixed: (shape, schedule) to run instead of the autotuner's pick."""
     from hydro_gb300 import cases
 
     sizes = cases.batch_sizes(count, seed=4)
@@ -331,7 +332,11 @@ def batch_run(hg, count, steps, tune_steps, l1_sample):
     try:
         for k, pr in enumerate(probs):
             b.upload(k, *pr)
-        best, times = b.autotune(cfg, steps=tune_steps)
+        if fixed is None:
+            best, times = b.autotune(cfg, steps=tune_steps)
+        else:
+            b.set_schedule(*fixed)
+            times = np.zeros((0, 0))
         l0 = hg.kernel_launches()
         info = b.run(cfg, steps)
         launches = hg.kernel_launches() - l0
@@ -525,6 +530,8 @@ def main():
     ap.add_argument("--no-costs", action="store_true", help="skip the learned start's per-face cost parts")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=300)
+    ap.add_argument("--batch-schedule", default=None,
+                    help="SHAPE,SCHEDULE: run the batch with this pair instead of the autotuner's pick")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -595,7 +602,8 @@ def main():
                 "conservation_final"]["mass"]
 
     e2e = None if args.no_e2e else e2e_run(hg, state, m, n, K)
-    batch = None if args.no_batch else batch_run(hg, args.batch_count, args.batch_steps, 5, 8)
+    fixed = tuple(int(x) for x in args.batch_schedule.split(",")) if args.batch_schedule else None
+    batch = None if args.no_batch else batch_run(hg, args.batch_count, args.batch_steps, 5, 8, fixed)
     shear = None if args.no_shear else shear_suite(hg, m, n, K, W, tune, args.stats_steps)
     g2d = None if args.no_g2d else g2d_suite(hg, state, m, n, K, k64, W, tune, args.stats_steps)
     mf = None if args.no_mf else mf_suite(hg, peak, cpu=not args.no_cpu)
