@@ -6,9 +6,11 @@
 // path (the acoustic shortcut is skipped), one thread per face, full warps:
 //   * the network: features and the three BF16 MMA layers (warp_mlp_outline);
 //   * the exact Riemann solve (q1d_star_exact, the Newton iteration with the
-//     FP64 fallback) from the reference's start and from the network's start,
-//     with the iterations each needs: their difference over the iterations
-//     saved is the cost of one FP32 Newton iteration;
+//     FP64 fallback) from the reference's start (half the tangent
+//     intersection), from the network's start and from the FP32 form's own
+//     start (the tangent intersection itself), with the iterations each needs:
+//     the difference of the first two over the iterations saved is the cost of
+//     one FP32 Newton iteration;
 //   * the nonlinear GRP derivatives and fluxes after the solve (q1d_waves,
 //     q1d_derivs), as the time of solve + derivatives less the solve.
 // Each kernel is timed with CUDA events over all faces, after one untimed run,
@@ -75,10 +77,11 @@ __global__ void __launch_bounds__(256) k_cost_mlp(int n, unsigned long long seed
 }
 
 // the exact solve (DERIVS: and the nonlinear GRP derivatives and fluxes)
+// (p_start null: every face starts from `start`, -2 the reference's start, -1 the FP32 form's)
 template <bool DERIVS>
 __global__ void __launch_bounds__(256) k_cost_solve(int n, unsigned long long seed, Gas<float> G, float tau,
-                                                    const float* __restrict__ p_start, int* __restrict__ iters,
-                                                    float* __restrict__ sink)
+                                                    const float* __restrict__ p_start, float start,
+                                                    int* __restrict__ iters, float* __restrict__ sink)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -91,7 +94,7 @@ __global__ void __launch_bounds__(256) k_cost_solve(int n, unsigned long long se
     S.acoustic = 0;
     StarInfo st;
     st.fallback = 0;
-    q1d_star_exact<float>(L, R, G, S, st, p_start ? p_start[i] : -1.f);
+    q1d_star_exact<float>(L, R, G, S, st, p_start ? p_start[i] : start);
     float out = S.p_star + S.u_star;
     if constexpr (DERIVS) {
         q1d_waves(L, R, G, S);
@@ -112,7 +115,7 @@ using namespace hydro;
 extern "C" int hydro_learned_costs(const float* params, int nfaces, unsigned long long seed, double gamma,
                                    double* out)
 {
-    memset(out, 0, sizeof(double) * 8);
+    memset(out, 0, sizeof(double) * 10);
     if (nfaces < 32 || !params) {
         set_error("learned_costs: at least 32 faces and the network's parameters");
         return -1;
@@ -125,8 +128,8 @@ extern "C" int hydro_learned_costs(const float* params, int nfaces, unsigned lon
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     int rc = -1;
     std::vector<int> it(n);
-    float ms[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    double mean_it[2] = {0.0, 0.0};
+    float ms[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double mean_it[3] = {0.0, 0.0, 0.0};
     Gas<float> G;
     fill_gas_params(G, gamma, 1e-9);
     const dim3 grid((n + 255) / 256), block(256);
@@ -144,17 +147,18 @@ extern "C" int hydro_learned_costs(const float* params, int nfaces, unsigned lon
     k_mlp_image<<<1, 256>>>(frag, prm, img);
     count_launch(2);
     // each kernel: one untimed run, then REPS timed back to back (launch gaps amortised)
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < 7; ++k) {
         constexpr int REPS = 5;
         for (int rep = 0; rep <= REPS; ++rep) {
             if (rep == 1)
                 cudaEventRecord(e0);
             switch (k) {
             case 0: k_cost_mlp<<<grid, block>>>(n, seed, G, img, p_start); break;
-            case 1: k_cost_solve<false><<<grid, block>>>(n, seed, G, 1e-4f, nullptr, iters, sink); break;
-            case 2: k_cost_solve<false><<<grid, block>>>(n, seed, G, 1e-4f, p_start, iters, sink); break;
-            case 3: k_cost_solve<true><<<grid, block>>>(n, seed, G, 1e-4f, nullptr, iters, sink); break;
-            case 4: k_cost_solve<true><<<grid, block>>>(n, seed, G, 1e-4f, p_start, iters, sink); break;
+            case 1: k_cost_solve<false><<<grid, block>>>(n, seed, G, 1e-4f, nullptr, -2.f, iters, sink); break;
+            case 2: k_cost_solve<false><<<grid, block>>>(n, seed, G, 1e-4f, p_start, -2.f, iters, sink); break;
+            case 3: k_cost_solve<true><<<grid, block>>>(n, seed, G, 1e-4f, nullptr, -2.f, iters, sink); break;
+            case 4: k_cost_solve<true><<<grid, block>>>(n, seed, G, 1e-4f, p_start, -2.f, iters, sink); break;
+            case 6: k_cost_solve<false><<<grid, block>>>(n, seed, G, 1e-4f, nullptr, -1.f, iters, sink); break;
             default: k_cost_gen<<<grid, block>>>(n, seed, G, sink); break;
             }
             count_launch();
@@ -164,13 +168,13 @@ extern "C" int hydro_learned_costs(const float* params, int nfaces, unsigned lon
             goto done;
         cudaEventElapsedTime(&ms[k], e0, e1);
         ms[k] /= REPS;
-        if (k == 1 || k == 2) {
+        if (k == 1 || k == 2 || k == 6) {
             if (!cuda_ok(cudaMemcpy(it.data(), iters, sizeof(int) * n, cudaMemcpyDeviceToHost), "costs"))
                 goto done;
             double s = 0.0;
             for (int v : it)
                 s += v;
-            mean_it[k - 1] = s / n;
+            mean_it[k == 6 ? 2 : k - 1] = s / n;
         }
     }
     {
@@ -185,6 +189,8 @@ extern "C" int hydro_learned_costs(const float* params, int nfaces, unsigned lon
         out[5] = (mean_it[0] - mean_it[1]) > 0.0 ? (out[1] - out[3]) / (mean_it[0] - mean_it[1]) : 0.0;
         out[6] = (ms[3] - ms[1]) * per;                   // GRP derivatives and fluxes after the solve
         out[7] = (ms[3] - g) * per;                       // the whole exact face, reference start
+        out[8] = (ms[6] - g) * per;                       // exact solve, the FP32 form's own start
+        out[9] = mean_it[2];                              // its Newton iterations per face
         rc = 0;
     }
 done:

@@ -272,10 +272,19 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
     return code;
 }
 
+// The learned start runs only on faces whose jump is at least this strong
+// (relative pressure jump |pL - pR| / (pL + pR) plus velocity jump
+// |uL - uR| / (cL + cR)).  Below it the tangent-intersection start of the
+// FP32 Newton iteration is within a few per cent of the root (its error is of
+// second order in the jump) and converges in 0-1 iterations, which the
+// network's start does not beat.
+constexpr float LEARNED_JUMP_MIN = 0.1f;
+
 // Learned starting pressure of the exact solver for every lane of the warp
-// whose face is not a uniform pair (warp-collective: all 32 lanes call it;
-// rows: only lanes below it are active).  Returns -1 where no guess applies
-// (uniform pair, inactive lane, a pair that would generate vacuum, a
+// whose face is not a uniform pair and has a strong jump (warp-collective: all
+// 32 lanes call it; rows: only lanes below it are active; the network is not
+// run at all when no lane needs it).  Returns -1 where no guess applies
+// (uniform pair, weak jump, inactive lane, a pair that would generate vacuum, a
 // non-finite prediction).
 __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<float>& Rr, bool active,
                                                const Gas<float>& G, const MlpShared& M, int rows)
@@ -283,7 +292,9 @@ __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<
     const float cL = sqrtf(G.g * L.p / L.rho), cR = sqrtf(G.g * Rr.p / Rr.rho);
     const float dist = sqrtf((L.rho - Rr.rho) * (L.rho - Rr.rho) + (L.u - Rr.u) * (L.u - Rr.u) +
                              (L.p - Rr.p) * (L.p - Rr.p));
-    const bool need = active && !StarPolicy<float>::uniform(dist, L.rho + Rr.rho + L.p + Rr.p + fabsf(L.u) + fabsf(Rr.u), G);
+    const float jump = fabsf(L.p - Rr.p) / (L.p + Rr.p) + fabsf(L.u - Rr.u) / (cL + cR);
+    const bool need = active && jump >= LEARNED_JUMP_MIN &&
+                      !StarPolicy<float>::uniform(dist, L.rho + Rr.rho + L.p + Rr.p + fabsf(L.u) + fabsf(Rr.u), G);
     float pg = -1.f;
     if (__any_sync(0xffffffffu, need)) {
         float x[6];

@@ -414,15 +414,17 @@ def fp64_peak() -> float:
 
 LEARNED_COST_KEYS = ("network_ns_per_face", "solve_ns_per_face_reference_start", "iters_reference_start",
                      "solve_ns_per_face_learned_start", "iters_learned_start", "ns_per_newton_iteration",
-                     "grp_derivatives_ns_per_face", "exact_face_ns_per_face")
+                     "grp_derivatives_ns_per_face", "exact_face_ns_per_face", "solve_ns_per_face_fp32_start",
+                     "iters_fp32_start")
 
 
 def learned_costs(params=None, nfaces: int = 1 << 20, seed: int = 7, gamma: float = 1.4) -> dict:
     """What the learned start costs and saves per face in the FP32 form's device
-    code (hydro_learned_costs): the network pass, the exact solve from either
-    start with its iterations, one Newton iteration, the GRP derivatives."""
+    code (hydro_learned_costs): the network pass, the exact solve from the
+    reference's, the network's and the FP32 form's own start with their
+    iterations, one Newton iteration, the GRP derivatives."""
     prm = np.ascontiguousarray(load_weights() if params is None else params, np.float32)
-    out = (ctypes.c_double * 8)()
+    out = (ctypes.c_double * len(LEARNED_COST_KEYS))()
     L = lib()
     L.hydro_learned_costs.restype = ctypes.c_int
     L.hydro_learned_costs.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_ulonglong,

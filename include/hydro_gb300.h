@@ -211,12 +211,14 @@ int hydro2d_set_mlp(hydro2d_t *h, const float *params);
 /* What the learned start costs and saves in the FP32 form's device code, on
  * nfaces (rounded down to a multiple of 32, at least 32) seeded Riemann pairs
  * with the four-quadrant data's ranges, all through the exact path, one thread
- * per face.  out[8]: ns per face of the network (features + three BF16 MMA
- * layers); of the exact solve from the reference's start; its mean Newton
- * iterations; of the exact solve from the network's start (network excluded);
- * its mean iterations; ns per FP32 Newton iteration (the solves' difference
- * over the iterations saved); ns per face of the nonlinear GRP derivatives and
- * fluxes after the solve; of the whole exact face from the reference's start. */
+ * per face.  out[10]: ns per face of the network (features + three BF16 MMA
+ * layers); of the exact solve from the reference's start (half the tangent
+ * intersection); its mean Newton iterations; of the exact solve from the
+ * network's start (network excluded); its mean iterations; ns per FP32 Newton
+ * iteration (the solves' difference over the iterations saved); ns per face of
+ * the nonlinear GRP derivatives and fluxes after the solve; of the whole exact
+ * face from the reference's start; of the exact solve from the FP32 form's own
+ * start (the tangent intersection); its mean iterations. */
 int hydro_learned_costs(const float *params, int nfaces, unsigned long long seed, double gamma, double *out);
 /* ---- batched problems (no reference counterpart) --------------------------
  * Many independent 2D unsplit GRP problems of uneven grid size m x n on the
