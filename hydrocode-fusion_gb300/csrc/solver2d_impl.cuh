@@ -50,8 +50,7 @@ struct StepVariant {
 template <typename R, int TJ, int TI, int NT, int MINB, bool LEARNED = false, int RS = 0>
 StepVariant<R> step_variant()
 {
-    return StepVariant<R>{TJ, TI, NT, MINB,
-                          LEARNED ? UnsplitSmem<R, TJ, TI>::bytes_learned : UnsplitSmem<R, TJ, TI>::bytes,
+    return StepVariant<R>{TJ, TI, NT, MINB, UnsplitSmem<R, TJ, TI>::bytes,
                           (const void*)k_step_unsplit<R, TJ, TI, NT, MINB, LEARNED, RS>, 0, 0, {}};
 }
 

@@ -272,31 +272,32 @@ __device__ __forceinline__ int solve_face(const Side<R>& L, const Side<R>& Rr, c
     return code;
 }
 
-// The learned start runs only on faces whose jump is at least this strong
-// (relative pressure jump |pL - pR| / (pL + pR) plus velocity jump
-// |uL - uR| / (cL + cR)).  Below it the tangent-intersection start of the
-// FP32 Newton iteration is within a few per cent of the root (its error is of
-// second order in the jump) and converges in 0-1 iterations, which the
-// network's start does not beat.
-constexpr float LEARNED_JUMP_MIN = 0.1f;
+// The learned start runs only on faces with a strong jump:
+//   (dp / (pL + pR))^2 + du^2 / (gamma (pL/rhoL + pR/rhoR)) >= LEARNED_JUMP2_MIN
+// (dp, du the pressure and velocity jumps; the second term is the squared
+// velocity jump over the sound speeds' root-sum-square), decided with
+// multiplications only.  Below it the tangent-intersection start of the FP32
+// Newton iteration is within a few per cent of the root (its error is of second
+// order in the jump) and converges in 0-1 iterations, which the network's start
+// does not beat.  A strong jump is never a uniform pair (that threshold is a
+// relative 1e-6).
+constexpr float LEARNED_JUMP2_MIN = 0.005f;
 
 // Learned starting pressure of the exact solver for every lane of the warp
-// whose face is not a uniform pair and has a strong jump (warp-collective: all
-// 32 lanes call it; rows: only lanes below it are active; the network is not
-// run at all when no lane needs it).  Returns -1 where no guess applies
-// (uniform pair, weak jump, inactive lane, a pair that would generate vacuum, a
-// non-finite prediction).
+// whose face has a strong jump (warp-collective: all 32 lanes call it; rows:
+// only lanes below it are active; the network is not run at all, nor the sound
+// speeds taken, when no lane needs it).  Returns -1 where no guess applies
+// (weak jump, inactive lane, a pair that would generate vacuum, a non-finite
+// prediction).
 __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<float>& Rr, bool active,
                                                const Gas<float>& G, const MlpShared& M, int rows)
 {
-    const float cL = sqrtf(G.g * L.p / L.rho), cR = sqrtf(G.g * Rr.p / Rr.rho);
-    const float dist = sqrtf((L.rho - Rr.rho) * (L.rho - Rr.rho) + (L.u - Rr.u) * (L.u - Rr.u) +
-                             (L.p - Rr.p) * (L.p - Rr.p));
-    const float jump = fabsf(L.p - Rr.p) / (L.p + Rr.p) + fabsf(L.u - Rr.u) / (cL + cR);
-    const bool need = active && jump >= LEARNED_JUMP_MIN &&
-                      !StarPolicy<float>::uniform(dist, L.rho + Rr.rho + L.p + Rr.p + fabsf(L.u) + fabsf(Rr.u), G);
+    const float sp = L.p + Rr.p, dp = L.p - Rr.p, du = L.u - Rr.u;
+    const float w = G.g * (L.p * Rr.rho + Rr.p * L.rho);  // gamma (pL/rhoL + pR/rhoR) rhoL rhoR
+    const bool need = active && dp * dp * w + du * du * (L.rho * Rr.rho) * (sp * sp) >= LEARNED_JUMP2_MIN * (sp * sp) * w;
     float pg = -1.f;
     if (__any_sync(0xffffffffu, need)) {
+        const float cL = sqrtf(G.g * L.p / L.rho), cR = sqrtf(G.g * Rr.p / Rr.rho);
         float x[6];
         float pbar = mlp_features(L.rho, L.u, L.p, cL, Rr.rho, Rr.u, Rr.p, cR, x);
         if (!need)
@@ -761,16 +762,16 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const Gas<R>&
     tile_body<R, TJ, TI, NT, LEARNED, false, RS>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, Mlp);
 }
 
+// The learned form reads the network's image from global memory (through L1):
+// one CTA per tile would otherwise copy its 11.8 KB into shared memory per tile.
 template <typename R, int TJ, int TI, int NT, int MINB = 1, bool LEARNED = false, int RS = 0>
 __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant__ StepArgs<R> a)
 {
-    using SM = UnsplitSmem<R, TJ, TI>;
     if (halt_prologue(a.ctl, a.seq))
         return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    MlpShared& Mlp = *reinterpret_cast<MlpShared*>(smem_raw + SM::mlp_off);
-    if (LEARNED)
-        mlp_load_shared(Mlp, a.mlp_frag, a.mlp_prm, threadIdx.x, NT);
+    // (the plain form never reads it)
+    const MlpShared& Mlp = *reinterpret_cast<const MlpShared*>(LEARNED ? a.mlp_img : (const void*)smem_raw);
     unsplit_tile<R, TJ, TI, NT, LEARNED, RS>(a, a.G, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
 }
 
