@@ -372,6 +372,32 @@ struct StageLayout {
 //     J0-2.., columns I0-X.., pitch BW) at W and the 8 previous-slope planes
 //     (rows J0-1.., same columns) at B; only the ghost cells of tiles at the
 //     domain edge are gathered.  FX may alias B (B is dead after phase 2).
+// Four consecutive values of a tile's shared-memory 4-vectors (16-byte aligned):
+// one 16-byte shared load or store in FP32, two in FP64.
+template <typename R>
+struct Quad {
+    R a, b, c, d;
+};
+__device__ __forceinline__ Quad<float> lds4(const float* p)
+{
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    return {t.x, t.y, t.z, t.w};
+}
+__device__ __forceinline__ Quad<double> lds4(const double* p)
+{
+    const double2 t0 = reinterpret_cast<const double2*>(p)[0], t1 = reinterpret_cast<const double2*>(p)[1];
+    return {t0.x, t0.y, t1.x, t1.y};
+}
+__device__ __forceinline__ void sts4(float* p, float a, float b, float c, float d)
+{
+    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void sts4(double* p, double a, double b, double c, double d)
+{
+    reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+    reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+}
+
 template <typename R, int TJ, int TI, int NT, bool LEARNED, bool STAGED, int RS = 0>
 __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
                                           R* __restrict__ W,
@@ -397,10 +423,17 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
     // value (lj, li) = cell (J0-2+lj, I0-2+li)
     constexpr int WP = STAGED ? SL::BW : SM::WI;
     constexpr int WO = STAGED ? SL::X - 2 : 0;
+    // W planar (plane, row, column), as the TMA boxes deliver it; S, FX and FY
+    // as two planes of 4-vectors per cell or face (x-slopes | y-slopes,
+    // fluxes | t+tau interface values), so that the four components a side or a
+    // face needs are one vector access (lds4 / sts4)
 #define Wx(k, lj, li) W[((k) * WJ + (lj)) * WP + (li) + WO]
-#define Sx(k, sj, si) S[((k) * SJ + (sj)) * SI + (si)]
-#define FXx(k, fj, fi) FX[((k) * (TJ + 1) + (fj)) * TI + (fi)]
-#define FYx(k, gj, gi) FY[((k) * TJ + (gj)) * (TI + 1) + (gi)]
+#define S4(p, sj, si) (S + (((p) * SJ + (sj)) * SI + (si)) * 4)
+#define FX4(p, fj, fi) (FX + (((p) * (TJ + 1) + (fj)) * TI + (fi)) * 4)
+#define FY4(p, gj, gi) (FY + (((p) * TJ + (gj)) * (TI + 1) + (gi)) * 4)
+#define Sx(k, sj, si) S4((k) >> 2, sj, si)[(k) & 3]
+#define FXx(k, fj, fi) FX4((k) >> 2, fj, fi)[(k) & 3]
+#define FYx(k, gj, gi) FY4((k) >> 2, gj, gi)[(k) & 3]
 
     // 1. values with a 2-cell halo (staged: only the ghosts of edge tiles)
     constexpr int WI = SM::WI;
@@ -449,6 +482,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
             o = slope_index(a, j, i);
         // staged previous slopes: plane k at B[(k * BJ + sj) * BW + si - 1 + X]
         const R* bs = STAGED ? B + sj * SL::BW + si - 1 + SL::X : nullptr;
+        R sxv[4], syv[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             R ps = R(0), pt = R(0);
@@ -460,9 +494,11 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                          a.alpha, a.find_x, ps);
             R sy = limit(Wx(k, sj + 1, si), Wx(k, sj + 1, si + 1), Wx(k, sj + 1, si + 2), a.hy, a.inv_hy, a.pow2_y,
                          a.alpha, a.find_y, pt);
-            Sx(k, sj, si) = sx;
-            Sx(4 + k, sj, si) = sy;
+            sxv[k] = sx;
+            syv[k] = sy;
         }
+        sts4(S4(0, sj, si), sxv[0], sxv[1], sxv[2], sxv[3]);
+        sts4(S4(1, sj, si), syv[0], syv[1], syv[2], syv[3]);
     }
     __syncthreads();
 
@@ -529,14 +565,20 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
             lj = fj; li = fi;
             j = J0 + fj; i = I0 + fi;
             // left cell (j-1): slopes at (fj, fi+1), values at (fj+1, fi+2)
-            L.drho = Sx(0, fj, fi + 1); L.du = Sx(1, fj, fi + 1); L.dv = Sx(2, fj, fi + 1); L.dp = Sx(3, fj, fi + 1);
-            L.trho = Sx(4, fj, fi + 1); L.tu = Sx(5, fj, fi + 1); L.tv = Sx(6, fj, fi + 1); L.tp = Sx(7, fj, fi + 1);
+            {
+                const Quad<R> d = lds4(S4(0, fj, fi + 1)), t = lds4(S4(1, fj, fi + 1));
+                L.drho = d.a; L.du = d.b; L.dv = d.c; L.dp = d.d;
+                L.trho = t.a; L.tu = t.b; L.tv = t.c; L.tp = t.d;
+            }
             L.rho = Wx(0, fj + 1, fi + 2) + a.hhx * L.drho;
             L.u = Wx(1, fj + 1, fi + 2) + a.hhx * L.du;
             L.v = Wx(2, fj + 1, fi + 2) + a.hhx * L.dv;
             L.p = Wx(3, fj + 1, fi + 2) + a.hhx * L.dp;
-            Rr.drho = Sx(0, fj + 1, fi + 1); Rr.du = Sx(1, fj + 1, fi + 1); Rr.dv = Sx(2, fj + 1, fi + 1); Rr.dp = Sx(3, fj + 1, fi + 1);
-            Rr.trho = Sx(4, fj + 1, fi + 1); Rr.tu = Sx(5, fj + 1, fi + 1); Rr.tv = Sx(6, fj + 1, fi + 1); Rr.tp = Sx(7, fj + 1, fi + 1);
+            {
+                const Quad<R> d = lds4(S4(0, fj + 1, fi + 1)), t = lds4(S4(1, fj + 1, fi + 1));
+                Rr.drho = d.a; Rr.du = d.b; Rr.dv = d.c; Rr.dp = d.d;
+                Rr.trho = t.a; Rr.tu = t.b; Rr.tv = t.c; Rr.tp = t.d;
+            }
             Rr.rho = Wx(0, fj + 2, fi + 2) - a.hhx * Rr.drho;
             Rr.u = Wx(1, fj + 2, fi + 2) - a.hhx * Rr.du;
             Rr.v = Wx(2, fj + 2, fi + 2) - a.hhx * Rr.dv;
@@ -550,8 +592,9 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         // lower cell (i-1): slopes at (gj+1, gi), values at (gj+2, gi+1); rotated to the +y normal frame:
         // normal velocity v, tangential -u; normal derivatives are the y-slopes, tangential the negated x-slopes
         {
-            R t0 = Sx(4, gj + 1, gi), t1 = Sx(5, gj + 1, gi), t2 = Sx(6, gj + 1, gi), t3 = Sx(7, gj + 1, gi);
-            R s0 = Sx(0, gj + 1, gi), s1 = Sx(1, gj + 1, gi), s2 = Sx(2, gj + 1, gi), s3 = Sx(3, gj + 1, gi);
+            const Quad<R> tq = lds4(S4(1, gj + 1, gi)), sq = lds4(S4(0, gj + 1, gi));
+            R t0 = tq.a, t1 = tq.b, t2 = tq.c, t3 = tq.d;
+            R s0 = sq.a, s1 = sq.b, s2 = sq.c, s3 = sq.d;
             R rr = Wx(0, gj + 2, gi + 1) + a.hhy * t0;
             R uu = Wx(1, gj + 2, gi + 1) + a.hhy * t1;
             R vv = Wx(2, gj + 2, gi + 1) + a.hhy * t2;
@@ -561,8 +604,9 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
             L.trho = -s0; L.tu = -s2; L.tv = s1; L.tp = -s3;
         }
         {
-            R t0 = Sx(4, gj + 1, gi + 1), t1 = Sx(5, gj + 1, gi + 1), t2 = Sx(6, gj + 1, gi + 1), t3 = Sx(7, gj + 1, gi + 1);
-            R s0 = Sx(0, gj + 1, gi + 1), s1 = Sx(1, gj + 1, gi + 1), s2 = Sx(2, gj + 1, gi + 1), s3 = Sx(3, gj + 1, gi + 1);
+            const Quad<R> tq = lds4(S4(1, gj + 1, gi + 1)), sq = lds4(S4(0, gj + 1, gi + 1));
+            R t0 = tq.a, t1 = tq.b, t2 = tq.c, t3 = tq.d;
+            R s0 = sq.a, s1 = sq.b, s2 = sq.c, s3 = sq.d;
             R rr = Wx(0, gj + 2, gi + 2) - a.hhy * t0;
             R uu = Wx(1, gj + 2, gi + 2) - a.hhy * t1;
             R vv = Wx(2, gj + 2, gi + 2) - a.hhy * t2;
@@ -595,18 +639,12 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         }
         if (!ydir) {
             report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                FXx(k, lj, li) = o.F[k];
-                FXx(4 + k, lj, li) = o.I[k];
-            }
+            sts4(FX4(0, lj, li), o.F[0], o.F[1], o.F[2], o.F[3]);
+            sts4(FX4(1, lj, li), o.I[0], o.I[1], o.I[2], o.I[3]);
         } else {
             report_face(a.ctl, slot, 1, (unsigned long long)j * (n + 1) + i, code);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                FYx(k, lj, li) = o.F[k];
-                FYx(4 + k, lj, li) = o.I[k];
-            }
+            sts4(FY4(0, lj, li), o.F[0], o.F[1], o.F[2], o.F[3]);
+            sts4(FY4(1, lj, li), o.I[0], o.I[1], o.I[2], o.I[3]);
         }
     };
     // pass A: warp-uniform rounds so the queue appends are warp-aggregated
@@ -683,18 +721,12 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                 const int code = solve_face_fp64_retry<RS>(L, Rr, G.g64, G.eps64, G.dist2_max, (double)a.tau, ydir, o);
                 if (!ydir) {
                     report_face(a.ctl, slot, 0, (unsigned long long)i * (m + 1) + j, code);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        FXx(k, lj, li) = o.F[k];
-                        FXx(4 + k, lj, li) = o.I[k];
-                    }
+                    sts4(FX4(0, lj, li), o.F[0], o.F[1], o.F[2], o.F[3]);
+                    sts4(FX4(1, lj, li), o.I[0], o.I[1], o.I[2], o.I[3]);
                 } else {
                     report_face(a.ctl, slot, 1, (unsigned long long)j * (n + 1) + i, code);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        FYx(k, lj, li) = o.F[k];
-                        FYx(4 + k, lj, li) = o.I[k];
-                    }
+                    sts4(FY4(0, lj, li), o.F[0], o.F[1], o.F[2], o.F[3]);
+                    sts4(FY4(1, lj, li), o.I[0], o.I[1], o.I[2], o.I[3]);
                 }
             }
             __syncthreads();
@@ -720,10 +752,13 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
             E = Wx(4, cj + 2, ci + 2);
         else
             E = a.src_w[4 * a.plane + o];
-        R mom_x = rho * uu - a.nu * (FXx(1, cj + 1, ci) - FXx(1, cj, ci)) - a.mu * (FYx(1, cj, ci + 1) - FYx(1, cj, ci));
-        R mom_y = rho * vv - a.nu * (FXx(2, cj + 1, ci) - FXx(2, cj, ci)) - a.mu * (FYx(2, cj, ci + 1) - FYx(2, cj, ci));
-        R ene = rho * E - a.nu * (FXx(3, cj + 1, ci) - FXx(3, cj, ci)) - a.mu * (FYx(3, cj, ci + 1) - FYx(3, cj, ci));
-        rho += -a.nu * (FXx(0, cj + 1, ci) - FXx(0, cj, ci)) - a.mu * (FYx(0, cj, ci + 1) - FYx(0, cj, ci));
+        // fluxes of the cell's four faces (x: rows cj, cj+1; y: columns ci, ci+1)
+        const Quad<R> fx0 = lds4(FX4(0, cj, ci)), fx1 = lds4(FX4(0, cj + 1, ci));
+        const Quad<R> fy0 = lds4(FY4(0, cj, ci)), fy1 = lds4(FY4(0, cj, ci + 1));
+        R mom_x = rho * uu - a.nu * (fx1.b - fx0.b) - a.mu * (fy1.b - fy0.b);
+        R mom_y = rho * vv - a.nu * (fx1.c - fx0.c) - a.mu * (fy1.c - fy0.c);
+        R ene = rho * E - a.nu * (fx1.d - fx0.d) - a.mu * (fy1.d - fy0.d);
+        rho += -a.nu * (fx1.a - fx0.a) - a.mu * (fy1.a - fy0.a);
         R un = mom_x / rho, vn = mom_y / rho, En = ene / rho;
         R pn = (ene - R(0.5) * mom_x * un - R(0.5) * mom_y * vn) * G.gm1;
         if (pn < G.eps || rho < G.eps)
@@ -733,10 +768,17 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         a.dst_w[2 * a.plane + o] = vn;
         a.dst_w[3 * a.plane + o] = pn;
         a.dst_w[4 * a.plane + o] = En;
+        {
+            // new slopes from the faces' t+tau interface values
+            const Quad<R> ix0 = lds4(FX4(1, cj, ci)), ix1 = lds4(FX4(1, cj + 1, ci));
+            const Quad<R> iy0 = lds4(FY4(1, cj, ci)), iy1 = lds4(FY4(1, cj, ci + 1));
+            const R dx[4] = {ix1.a - ix0.a, ix1.b - ix0.b, ix1.c - ix0.c, ix1.d - ix0.d};
+            const R dy[4] = {iy1.a - iy0.a, iy1.b - iy0.b, iy1.c - iy0.c, iy1.d - iy0.d};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            a.dst_s[k * a.plane + o] = div_h(FXx(4 + k, cj + 1, ci) - FXx(4 + k, cj, ci), a.hx, a.inv_hx, a.pow2_x);
-            a.dst_t[k * a.plane + o] = div_h(FYx(4 + k, cj, ci + 1) - FYx(4 + k, cj, ci), a.hy, a.inv_hy, a.pow2_y);
+            for (int k = 0; k < 4; ++k) {
+                a.dst_s[k * a.plane + o] = div_h(dx[k], a.hx, a.inv_hx, a.pow2_x);
+                a.dst_t[k * a.plane + o] = div_h(dy[k], a.hy, a.inv_hy, a.pow2_y);
+            }
         }
     }
     if (bad)
@@ -746,6 +788,9 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
 #undef Sx
 #undef FXx
 #undef FYx
+#undef S4
+#undef FX4
+#undef FY4
 }
 
 // The gathered tile with its shared-memory carve-up (W | S | FX | FY).
