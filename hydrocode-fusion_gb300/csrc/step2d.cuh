@@ -377,6 +377,7 @@ struct StageLayout {
 template <typename R>
 struct Quad {
     R a, b, c, d;
+    __device__ __forceinline__ R operator[](int k) const { return k == 0 ? a : (k == 1 ? b : (k == 2 ? c : d)); }
 };
 __device__ __forceinline__ Quad<float> lds4(const float* p)
 {
@@ -423,17 +424,27 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
     // value (lj, li) = cell (J0-2+lj, I0-2+li)
     constexpr int WP = STAGED ? SL::BW : SM::WI;
     constexpr int WO = STAGED ? SL::X - 2 : 0;
-    // W planar (plane, row, column), as the TMA boxes deliver it; S, FX and FY
+    // W of a TMA-staged tile planar (plane, row, column), as the boxes deliver
+    // it, and of a gathered tile one 4-vector (rho u v p) per cell; S, FX and FY
     // as two planes of 4-vectors per cell or face (x-slopes | y-slopes,
     // fluxes | t+tau interface values), so that the four components a side or a
     // face needs are one vector access (lds4 / sts4)
-#define Wx(k, lj, li) W[((k) * WJ + (lj)) * WP + (li) + WO]
+#define Wx(k, lj, li) (STAGED ? W[((k) * WJ + (lj)) * WP + (li) + WO] : W[((lj) * SM::WI + (li)) * 4 + (k)])
+#define W4(lj, li) (W + ((lj) * SM::WI + (li)) * 4)
 #define S4(p, sj, si) (S + (((p) * SJ + (sj)) * SI + (si)) * 4)
 #define FX4(p, fj, fi) (FX + (((p) * (TJ + 1) + (fj)) * TI + (fi)) * 4)
 #define FY4(p, gj, gi) (FY + (((p) * TJ + (gj)) * (TI + 1) + (gi)) * 4)
 #define Sx(k, sj, si) S4((k) >> 2, sj, si)[(k) & 3]
 #define FXx(k, fj, fi) FX4((k) >> 2, fj, fi)[(k) & 3]
 #define FYx(k, gj, gi) FY4((k) >> 2, gj, gi)[(k) & 3]
+
+    // rho u v p of value cell (lj, li)
+    auto wq = [&](int lj, int li) -> Quad<R> {
+        if constexpr (STAGED)
+            return {Wx(0, lj, li), Wx(1, lj, li), Wx(2, lj, li), Wx(3, lj, li)};
+        else
+            return lds4(W4(lj, li));
+    };
 
     // 1. values with a 2-cell halo (staged: only the ghosts of edge tiles)
     constexpr int WI = SM::WI;
@@ -445,9 +456,13 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                 continue;
             R w[4];
             load_prims(a, j, i, w);
+            if constexpr (STAGED) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                Wx(k, lj, li) = w[k];
+                for (int k = 0; k < 4; ++k)
+                    Wx(k, lj, li) = w[k];
+            } else {
+                sts4(W4(lj, li), w[0], w[1], w[2], w[3]);
+            }
         }
         __syncthreads();  // (an interior staged tile wrote nothing here)
     }
@@ -483,6 +498,9 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         // staged previous slopes: plane k at B[(k * BJ + sj) * BW + si - 1 + X]
         const R* bs = STAGED ? B + sj * SL::BW + si - 1 + SL::X : nullptr;
         R sxv[4], syv[4];
+        // the centre and its four neighbours along x (rows) and y (columns)
+        const Quad<R> wc = wq(sj + 1, si + 1), wxm = wq(sj, si + 1), wxp = wq(sj + 2, si + 1);
+        const Quad<R> wym = wq(sj + 1, si), wyp = wq(sj + 1, si + 2);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             R ps = R(0), pt = R(0);
@@ -490,10 +508,8 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                 ps = inside ? bs[k * SL::BJ * SL::BW] : a.src_s[k * a.plane + o];
             if (a.find_y)
                 pt = inside ? bs[(4 + k) * SL::BJ * SL::BW] : a.src_t[k * a.plane + o];
-            R sx = limit(Wx(k, sj, si + 1), Wx(k, sj + 1, si + 1), Wx(k, sj + 2, si + 1), a.hx, a.inv_hx, a.pow2_x,
-                         a.alpha, a.find_x, ps);
-            R sy = limit(Wx(k, sj + 1, si), Wx(k, sj + 1, si + 1), Wx(k, sj + 1, si + 2), a.hy, a.inv_hy, a.pow2_y,
-                         a.alpha, a.find_y, pt);
+            R sx = limit(wxm[k], wc[k], wxp[k], a.hx, a.inv_hx, a.pow2_x, a.alpha, a.find_x, ps);
+            R sy = limit(wym[k], wc[k], wyp[k], a.hy, a.inv_hy, a.pow2_y, a.alpha, a.find_y, pt);
             sxv[k] = sx;
             syv[k] = sy;
         }
@@ -570,19 +586,25 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                 L.drho = d.a; L.du = d.b; L.dv = d.c; L.dp = d.d;
                 L.trho = t.a; L.tu = t.b; L.tv = t.c; L.tp = t.d;
             }
-            L.rho = Wx(0, fj + 1, fi + 2) + a.hhx * L.drho;
-            L.u = Wx(1, fj + 1, fi + 2) + a.hhx * L.du;
-            L.v = Wx(2, fj + 1, fi + 2) + a.hhx * L.dv;
-            L.p = Wx(3, fj + 1, fi + 2) + a.hhx * L.dp;
+            {
+                const Quad<R> w = wq(fj + 1, fi + 2);
+                L.rho = w.a + a.hhx * L.drho;
+                L.u = w.b + a.hhx * L.du;
+                L.v = w.c + a.hhx * L.dv;
+                L.p = w.d + a.hhx * L.dp;
+            }
             {
                 const Quad<R> d = lds4(S4(0, fj + 1, fi + 1)), t = lds4(S4(1, fj + 1, fi + 1));
                 Rr.drho = d.a; Rr.du = d.b; Rr.dv = d.c; Rr.dp = d.d;
                 Rr.trho = t.a; Rr.tu = t.b; Rr.tv = t.c; Rr.tp = t.d;
             }
-            Rr.rho = Wx(0, fj + 2, fi + 2) - a.hhx * Rr.drho;
-            Rr.u = Wx(1, fj + 2, fi + 2) - a.hhx * Rr.du;
-            Rr.v = Wx(2, fj + 2, fi + 2) - a.hhx * Rr.dv;
-            Rr.p = Wx(3, fj + 2, fi + 2) - a.hhx * Rr.dp;
+            {
+                const Quad<R> w = wq(fj + 2, fi + 2);
+                Rr.rho = w.a - a.hhx * Rr.drho;
+                Rr.u = w.b - a.hhx * Rr.du;
+                Rr.v = w.c - a.hhx * Rr.dv;
+                Rr.p = w.d - a.hhx * Rr.dp;
+            }
             return !(j > m || i >= n);
         }
         const int g = f - NFX;
@@ -595,10 +617,11 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
             const Quad<R> tq = lds4(S4(1, gj + 1, gi)), sq = lds4(S4(0, gj + 1, gi));
             R t0 = tq.a, t1 = tq.b, t2 = tq.c, t3 = tq.d;
             R s0 = sq.a, s1 = sq.b, s2 = sq.c, s3 = sq.d;
-            R rr = Wx(0, gj + 2, gi + 1) + a.hhy * t0;
-            R uu = Wx(1, gj + 2, gi + 1) + a.hhy * t1;
-            R vv = Wx(2, gj + 2, gi + 1) + a.hhy * t2;
-            R pp = Wx(3, gj + 2, gi + 1) + a.hhy * t3;
+            const Quad<R> w = wq(gj + 2, gi + 1);
+            R rr = w.a + a.hhy * t0;
+            R uu = w.b + a.hhy * t1;
+            R vv = w.c + a.hhy * t2;
+            R pp = w.d + a.hhy * t3;
             L.rho = rr; L.u = vv; L.v = -uu; L.p = pp;
             L.drho = t0; L.du = t2; L.dv = -t1; L.dp = t3;
             L.trho = -s0; L.tu = -s2; L.tv = s1; L.tp = -s3;
@@ -607,10 +630,11 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
             const Quad<R> tq = lds4(S4(1, gj + 1, gi + 1)), sq = lds4(S4(0, gj + 1, gi + 1));
             R t0 = tq.a, t1 = tq.b, t2 = tq.c, t3 = tq.d;
             R s0 = sq.a, s1 = sq.b, s2 = sq.c, s3 = sq.d;
-            R rr = Wx(0, gj + 2, gi + 2) - a.hhy * t0;
-            R uu = Wx(1, gj + 2, gi + 2) - a.hhy * t1;
-            R vv = Wx(2, gj + 2, gi + 2) - a.hhy * t2;
-            R pp = Wx(3, gj + 2, gi + 2) - a.hhy * t3;
+            const Quad<R> w = wq(gj + 2, gi + 2);
+            R rr = w.a - a.hhy * t0;
+            R uu = w.b - a.hhy * t1;
+            R vv = w.c - a.hhy * t2;
+            R pp = w.d - a.hhy * t3;
             Rr.rho = rr; Rr.u = vv; Rr.v = -uu; Rr.p = pp;
             Rr.drho = t0; Rr.du = t2; Rr.dv = -t1; Rr.dp = t3;
             Rr.trho = -s0; Rr.tu = -s2; Rr.tv = s1; Rr.tp = -s3;
@@ -746,7 +770,8 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         if (j >= m || i >= n)
             continue;
         const size_t o = (size_t)j * a.ld + i;
-        R rho = Wx(0, cj + 2, ci + 2), uu = Wx(1, cj + 2, ci + 2), vv = Wx(2, cj + 2, ci + 2);
+        const Quad<R> wcell = wq(cj + 2, ci + 2);
+        R rho = wcell.a, uu = wcell.b, vv = wcell.c;
         R E;
         if constexpr (STAGED)
             E = Wx(4, cj + 2, ci + 2);
@@ -791,6 +816,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
 #undef S4
 #undef FX4
 #undef FY4
+#undef W4
 }
 
 // The gathered tile with its shared-memory carve-up (W | S | FX | FY).
