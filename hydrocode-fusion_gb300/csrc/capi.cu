@@ -325,13 +325,64 @@ HostPair* host_pair()
     return pp;
 }
 
+// The 2D entry points keep the last call's solver (its device buffers, kernel
+// set-up and network) for the next call with the same grid, form and interface
+// solver, as a memory pool keeps its blocks: a caller that runs the scheme
+// repeatedly pays the solver's set-up once.  HYDRO_SOLVER_CACHE=0 turns it off
+// (each call creates and frees its own); hydro_gb300_release_cache() frees the
+// kept solver.  The cache object is never destroyed: a solver still held at
+// exit goes with the process's CUDA context.
+struct SolverCache {
+    std::mutex mu;
+    Solver2DBase* s = nullptr;
+    int m = 0, n = 0, form = -1, rs = -1;
+};
+static SolverCache& solver_cache()
+{
+    static SolverCache* c = new SolverCache();
+    return *c;
+}
+static bool solver_cache_on()
+{
+    const char* e = getenv("HYDRO_SOLVER_CACHE");
+    return !(e && atoi(e) == 0);
+}
+static Solver2DBase* acquire_solver(int m, int n, int form, int rs)
+{
+    if (solver_cache_on()) {
+        SolverCache& c = solver_cache();
+        std::lock_guard<std::mutex> guard(c.mu);
+        if (c.s && c.m == m && c.n == n && c.form == form && c.rs == rs) {
+            Solver2DBase* s = c.s;
+            c.s = nullptr;  // one caller at a time uses it
+            return s;
+        }
+    }
+    return make_solver(m, n, form, rs);
+}
+static void release_solver(Solver2DBase* s, int m, int n, int form, int rs)
+{
+    Solver2DBase* old = s;
+    if (solver_cache_on()) {
+        SolverCache& c = solver_cache();
+        std::lock_guard<std::mutex> guard(c.mu);
+        old = c.s;
+        c.s = s;
+        c.m = m;
+        c.n = n;
+        c.form = form;
+        c.rs = rs;
+    }
+    delete old;
+}
+
 // Shared body of the two 2D scheme entry points.
 static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, double* cpu_time, int N_T, int* N_plot,
                          double time_plot[], int split)
 {
     const double t_all = config[1];
-    const int form = form_from_config(config);
-    Solver2DBase* s = make_solver(m, n, form, solver_from_config(config));
+    const int form = form_from_config(config), rs = solver_from_config(config);
+    Solver2DBase* s = acquire_solver(m, n, form, rs);
     if (!s) {
         fprintf(stderr, "hydro_gb300: cannot create the 2D solver: %s\n", hydro_gb300_last_error());
         exit(5);
@@ -365,7 +416,7 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
         fprintf(stderr, "hydro_gb300: download failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }
-    delete s;
+    release_solver(s, m, n, form, rs);
     auto scatter = [&](int k, const double* src) {
         parallel_rows(m, n, [&](int j0, int j1) {
             for (int j = j0; j < j1; ++j) {
@@ -413,6 +464,18 @@ extern "C" {
 
 const char* hydro_gb300_last_error(void) { return g_err.c_str(); }
 unsigned long long hydro_gb300_kernel_launches(void) { return g_launches.load(); }
+
+void hydro_gb300_release_cache(void)
+{
+    SolverCache& c = solver_cache();
+    Solver2DBase* old = nullptr;
+    {
+        std::lock_guard<std::mutex> guard(c.mu);
+        old = c.s;
+        c.s = nullptr;
+    }
+    delete old;
+}
 
 int hydro2d_create_ex(hydro2d_t** out, int m, int n, int form, int solver)
 {

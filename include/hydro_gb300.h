@@ -325,6 +325,12 @@ int hydro_grp2d_flux_mf(int nface, const double *in, double *out, int *status, c
    d2 <= this value. */
 double hydro_uniform_dist2_max(double eps);
 
+/* The 2D scheme entry points (GRP_solver_2D_[split_]EUL_source) keep the last
+   call's solver -- its device buffers, kernel set-up and network -- for the
+   next call with the same grid, form and interface solver (environment
+   HYDRO_SOLVER_CACHE=0: no solver is kept).  This frees the kept solver. */
+void hydro_gb300_release_cache(void);
+
 /* Number of CUDA kernels launched by this library since load (all solvers). */
 unsigned long long hydro_gb300_kernel_launches(void);
 /* Message of the last failing call in this thread ("" if none). */

@@ -100,3 +100,33 @@ def test_entry_row_copies_match_plane_api(gpu_lib, form, monkeypatch):
         s.close()
     for f, key in enumerate(("rho", "u", "v", "p", "E")):
         assert np.array_equal(data[nplot - 1, f], want[key]), key
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [None, 2])
+def test_2d_entry_kept_solver(gpu_lib, monkeypatch, form):
+    """The 2D entry keeps the last call's solver for the next call of the same
+    grid and form: repeated calls (the kept solver) give the same bits as a call
+    with the cache off (HYDRO_SOLVER_CACHE=0, a solver of its own), also after
+    a call of another size in between, and after hydro_gb300_release_cache."""
+    hg = gpu_lib
+    from hydro_gb300 import cases
+
+    m, n = 40, 36
+    rho, u, v, p = cases.four_quadrant(m, n, 6)
+    cfg = hg.config_2d(t_all=-1, steps=12, hx=1 / m, hy=1 / n, bx=-4, by=-4,
+                       **({} if form is None else {"form": form}))
+    other = cases.four_quadrant(24, 28, 7)
+    cfg_other = hg.config_2d(t_all=-1, steps=5, hx=1 / 24, hy=1 / 28, bx=-4, by=-4,
+                             **({} if form is None else {"form": form}))
+    monkeypatch.setenv("HYDRO_SOLVER_CACHE", "0")
+    ref = call_2d(hg.lib(), rho, u, v, p, 1.4, cfg, N_MAX=2)[0]
+    monkeypatch.delenv("HYDRO_SOLVER_CACHE")
+    runs = [call_2d(hg.lib(), rho, u, v, p, 1.4, cfg, N_MAX=2)[0] for _ in range(2)]
+    call_2d(hg.lib(), *other, 1.4, cfg_other, N_MAX=2)
+    runs.append(call_2d(hg.lib(), rho, u, v, p, 1.4, cfg, N_MAX=2)[0])
+    hg.lib().hydro_gb300_release_cache()
+    runs.append(call_2d(hg.lib(), rho, u, v, p, 1.4, cfg, N_MAX=2)[0])
+    for got in runs:
+        assert np.array_equal(got[1], ref[1])
+    hg.lib().hydro_gb300_release_cache()
