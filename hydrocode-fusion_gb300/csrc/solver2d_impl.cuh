@@ -590,13 +590,12 @@ public:
     // A host value in the state's precision, rounded as the FP32 forms' device
     // conversion rounds it (to nearest, a subnormal float result flushed to a
     // zero of its sign: those kernels are compiled with --use_fast_math).
+    // (a select, not a branch, so that the packing loops vectorise)
     static R to_state(double x)
     {
         if constexpr (sizeof(R) == 4) {
-            float f = (float)x;
-            if (f != 0.f && fabsf(f) < 1.17549435e-38f)
-                f = copysignf(0.f, f);
-            return f;
+            const float f = (float)x;
+            return fabsf(f) < 1.17549435e-38f ? copysignf(0.f, f) : f;
         } else {
             return x;
         }
