@@ -730,14 +730,20 @@ int hydro_batch_create(hydro_batch** out, int nprob, const int* m, const int* n)
         return -1;
     }
     for (const BatchShape& s : batch_shapes())
-        for (const void* k : {s.persistent, s.step})
+        for (const void* k : {s.persistent, s.step}) {
+            // tile shapes: the shared memory their MINB CTAs per SM need, the rest L1
+            int carve = s.carve;
+            cudaFuncAttributes fa;
+            if (!s.strip && cudaFuncGetAttributes(&fa, k) == cudaSuccess)
+                carve = carve_for(s.smem + fa.sharedSizeBytes, s.MINB);
             if (!cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem),
                          "smem attr") ||
-                !cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, s.carve),
+                !cuda_ok(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, carve),
                          "carveout attr")) {
                 delete b;
                 return -1;
             }
+        }
     *out = b;
     return 0;
 }

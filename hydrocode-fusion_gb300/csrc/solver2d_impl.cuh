@@ -33,6 +33,21 @@ namespace hydro {
 // tile (k_step_unsplit).  strip = 1: the FP32 strip kernel (k_step_strip,
 // strip2d.cuh), persistent with occ CTAs per SM, TJ = rows per work unit,
 // TI = columns a strip updates.
+// The smallest shared-memory carve-out (per cent of the largest, 228 KB) that
+// holds `ctas` CTAs of `bytes` shared memory each (the hardware keeps 1 KB per
+// CTA besides), so that the rest of the unified L1/shared storage is L1 for the
+// tile code's spills and the exact path's stack.  The percentage is rounded
+// down: the driver takes the smallest configuration at or above it.
+inline int carve_for(size_t bytes, int ctas)
+{
+    static const int cfg_kb[] = {0, 8, 16, 32, 64, 100, 132, 164, 196, 228};
+    const size_t need = (size_t)ctas * (bytes + 1024);
+    for (int kb : cfg_kb)
+        if ((size_t)kb * 1024 >= need)
+            return kb * 100 / 228;
+    return 100;
+}
+
 template <typename R>
 struct StepVariant {
     int TJ, TI, NT, MINB;
@@ -424,8 +439,11 @@ public:
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax),
                          "smem attr"))
                 return -1;
-            // the unified L1/shared storage: all of it as shared memory (several tile CTAs fit
-            // per SM), or part of it left as L1 (the strip kernel's register spills)
+            // the unified L1/shared storage: the shared memory the variant's CTAs need, the
+            // rest L1 (the gathered tiles: MINB CTAs per SM; the strip kernel: its own split;
+            // the persistent TMA kernels: all of it)
+            if (!v.strip && !v.tma)
+                v.carve = carve_for(v.smem + fa.sharedSizeBytes, v.MINB);
             if (!cuda_ok(cudaFuncSetAttribute(v.kern, cudaFuncAttributePreferredSharedMemoryCarveout, v.carve),
                          "carveout attr"))
                 return -1;
