@@ -147,12 +147,12 @@ __device__ __forceinline__ bool batch_tile_args(const BatchDev& B, int t, int st
 
 template <int TJ, int TI, int NT>
 __device__ __forceinline__ void batch_tile(const BatchDev& B, int t, int step, StepArgs<float>& sa, unsigned char* smem,
-                                           const MlpShared& M)
+                                           const MlpShared& M, bool last_tile = false)
 {
     int lt;
     if (batch_tile_args(B, t, step, sa, lt)) {
         const int nty = B.tiles_y[B.tile_prob[t]];
-        unsplit_tile<float, TJ, TI, NT, false>(sa, B.G, (lt % nty) * TI, (lt / nty) * TJ, smem, M);
+        unsplit_tile<float, TJ, TI, NT, false>(sa, B.G, (lt % nty) * TI, (lt / nty) * TJ, smem, M, last_tile);
     }
 }
 
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_step(const __grid_constant__
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ StepArgs<float> sa;
     const MlpShared& M = *reinterpret_cast<const MlpShared*>(smem_raw);
-    batch_tile<TJ, TI, NT>(B, B.order[blockIdx.x], step, sa, smem_raw, M);
+    batch_tile<TJ, TI, NT>(B, B.order[blockIdx.x], step, sa, smem_raw, M, true);
 }
 
 // ---------------------------------------------------------------------------

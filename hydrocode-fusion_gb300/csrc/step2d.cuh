@@ -403,7 +403,8 @@ template <typename R, int TJ, int TI, int NT, bool LEARNED, bool STAGED, int RS 
 __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
                                           R* __restrict__ W,
                                           const R* B, R* __restrict__ S, R* FX, R* __restrict__ FY,
-                                          unsigned short* __restrict__ Q, const MlpShared& Mlp)
+                                          unsigned short* __restrict__ Q, const MlpShared& Mlp,
+                                          bool last_tile = false)
 {
     static_assert(!(LEARNED && RS != 0), "the learned start is built for the quasi-1D interface solver");
     using SM = UnsplitSmem<R, TJ, TI>;
@@ -731,7 +732,8 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
                 atomicAdd(&a.ctl->newton_fallbacks, (unsigned long long)my_fb);
         }
     }
-    __syncthreads();
+    if (qn > 0)  // (block-uniform) pass B wrote faces that phase 4 reads
+        __syncthreads();
     if constexpr (sizeof(R) == 4) {
         const int nr = s_nretry < RETRY_MAX ? s_nretry : RETRY_MAX;
         if (nr > 0) {
@@ -808,7 +810,8 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
     }
     if (bad)
         atomicOr(&a.ctl->upd_bad[slot], 1u);
-    __syncthreads();
+    if (!last_tile)  // the CTA's next tile reuses the shared memory
+        __syncthreads();
 #undef Wx
 #undef Sx
 #undef FXx
@@ -822,7 +825,7 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
 // The gathered tile with its shared-memory carve-up (W | S | FX | FY).
 template <typename R, int TJ, int TI, int NT, bool LEARNED, int RS = 0>
 __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const Gas<R>& G, const int I0, const int J0,
-                                             unsigned char* smem_raw, const MlpShared& Mlp)
+                                             unsigned char* smem_raw, const MlpShared& Mlp, bool last_tile = false)
 {
     using SM = UnsplitSmem<R, TJ, TI>;
     R* W = reinterpret_cast<R*>(smem_raw);
@@ -830,7 +833,7 @@ __device__ __forceinline__ void unsplit_tile(const StepArgs<R>& a, const Gas<R>&
     R* FX = S + SM::nS;
     R* FY = FX + SM::nFX;
     unsigned short* Q = reinterpret_cast<unsigned short*>(smem_raw + SM::bytes_f);
-    tile_body<R, TJ, TI, NT, LEARNED, false, RS>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, Mlp);
+    tile_body<R, TJ, TI, NT, LEARNED, false, RS>(a, G, I0, J0, W, nullptr, S, FX, FY, Q, Mlp, last_tile);
 }
 
 // The learned form reads the network's image from global memory (through L1):
@@ -843,7 +846,7 @@ __global__ void __launch_bounds__(NT, MINB) k_step_unsplit(const __grid_constant
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // (the plain form never reads it)
     const MlpShared& Mlp = *reinterpret_cast<const MlpShared*>(LEARNED ? a.mlp_img : (const void*)smem_raw);
-    unsplit_tile<R, TJ, TI, NT, LEARNED, RS>(a, a.G, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp);
+    unsplit_tile<R, TJ, TI, NT, LEARNED, RS>(a, a.G, blockIdx.x * TI, blockIdx.y * TJ, smem_raw, Mlp, true);
 }
 
 // ---------------------------------------------------------------------------
