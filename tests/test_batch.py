@@ -158,6 +158,26 @@ def test_batch_against_fp64_oracle(gpu_lib, port):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("bx,by", [(-2, -7), (-24, -1), (-7, -2), (-1, -24)])
+def test_batch_boundaries_against_fp64_oracle(gpu_lib, port, bx, by):
+    """Every boundary kind the scheme reads (reflective -2, periodic -7, the
+    half-reflective -24, the fixed initial values -1), on the shape and
+    schedule the autotuner picks on the bench's batch (16x16 tiles, one launch
+    per step): each problem within the FP32 form's tolerance of the FP64
+    oracle run of its own grid."""
+    hg = gpu_lib
+    probs = _problems(hg)
+    cfg = _cfg(hg, bx, by)
+    got, info, _ = _run_batch(hg, probs, cfg, shape=2, schedule=4)
+    assert info.halted_problems == 0
+    for k, (m, n) in enumerate(SIZES):
+        c = hg.config_2d(t_all=-1, steps=STEPS, hx=1.0 / m, hy=1.0 / n, bx=bx, by=by)
+        want = port.run_2d(*probs[k], c)
+        for f in FIELDS:
+            assert rel_l1(got[k][f], want[f]) <= FP32_TOL, (k, f, rel_l1(got[k][f], want[f]))
+
+
+@pytest.mark.gpu
 def test_batch_schedules_and_shapes_agree(gpu_lib):
     """Each tile is computed once per step from the previous step's state, in
     any order, so the order cannot change a result: the persistent schedules
