@@ -17,6 +17,10 @@ CASES = [
     (33, 96, -24, -1, 8),
     # strips and row units with interior ones on both axes (the strip kernel's fast path)
     (150, 200, -4, -7, 9),
+    # a grid smaller than one tile and one strip unit
+    (3, 5, -4, -4, 12),
+    # one full strip and a strip of four columns, rows not a multiple of a unit
+    (61, 64, -2, -7, 13),
 ]
 STEPS = 12
 
