@@ -447,16 +447,28 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
             return lds4(W4(lj, li));
     };
 
+    // a tile whose halo lies inside the grid reads its cells directly (no
+    // boundary rule applies to any of them); block-uniform
+    const bool interior = J0 >= 2 && I0 >= 2 && J0 + TJ + 2 <= m && I0 + TI + 2 <= n;
+
     // 1. values with a 2-cell halo (staged: only the ghosts of edge tiles)
     constexpr int WI = SM::WI;
-    if (!STAGED || J0 < 2 || I0 < 2 || J0 + TJ + 2 > m || I0 + TI + 2 > n) {
+    if (!STAGED || !interior) {
         for (int idx = tid; idx < WJ * WI; idx += NT) {
             int lj = idx / WI, li = idx - lj * WI;
             const int j = J0 - 2 + lj, i = I0 - 2 + li;
             if (STAGED && j >= 0 && j < m && i >= 0 && i < n)
                 continue;
             R w[4];
-            load_prims(a, j, i, w);
+            if (!STAGED && interior) {
+                const size_t o = (size_t)j * a.ld + i;
+                w[0] = a.src_w[o];
+                w[1] = a.src_w[a.plane + o];
+                w[2] = a.src_w[2 * a.plane + o];
+                w[3] = a.src_w[3 * a.plane + o];
+            } else {
+                load_prims(a, j, i, w);
+            }
             if constexpr (STAGED) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
@@ -494,7 +506,9 @@ __device__ __forceinline__ void tile_body(const StepArgs<R>& a, const Gas<R>& G,
         int j = J0 - 1 + sj, i = I0 - 1 + si;
         const bool inside = STAGED && j >= 0 && j < m && i >= 0 && i < n;
         size_t o = 0;  // global index of the previous slopes, needed only when they are not staged
-        if (!inside)
+        if (!STAGED && interior)
+            o = (size_t)j * a.ld + i;
+        else if (!inside)
             o = slope_index(a, j, i);
         // staged previous slopes: plane k at B[(k * BJ + sj) * BW + si - 1 + X]
         const R* bs = STAGED ? B + sj * SL::BW + si - 1 + SL::X : nullptr;
