@@ -593,7 +593,12 @@ static __device__ __noinline__ void exact_riemann_fp64_fallback(float uL, float 
 template <> struct StarPolicy<float> {
     static __device__ __forceinline__ bool uniform(float dist, float scale, const Gas<float>& G)
     {
-        return dist < fmaxf(G.eps, 1e-6f * scale);
+        return dist < threshold(scale, G);
+    }
+    // the uniform-pair distance threshold, relative to the states' magnitude
+    static __device__ __forceinline__ float threshold(float scale, const Gas<float>& G)
+    {
+        return fmaxf(G.eps, 1e-6f * scale);
     }
     template <bool FUSED = true>  // (FP32: one form)
     static __device__ void solve(float uL, float uR, float pL, float pR, float cL, float cR, const Gas<float>& G,
@@ -705,15 +710,17 @@ __device__ __forceinline__ bool face_uniform(const Side<R>& L, const Side<R>& Rr
             d2 = d2 + (L.v - Rr.v) * (L.v - Rr.v);
         d2 = d2 + (p_L - p_R) * (p_L - p_R);
         return d2 <= G.dist2_max;
-    } else if constexpr (RS == 1) {
-        const R v_L = L.v, v_R = Rr.v;
-        R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) +
-                             (v_L - v_R) * (v_L - v_R) + (p_L - p_R) * (p_L - p_R));
-        return StarPolicy<R>::uniform(dist, rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R) +
-                                                M<R>::abs_(v_L) + M<R>::abs_(v_R), G);
     } else {
-        R dist = M<R>::sqrt_((rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R));
-        return StarPolicy<R>::uniform(dist, rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R), G);
+        // FP32: the squared distance against the squared threshold (as the strip
+        // kernel's packed test), no square root
+        R d2 = (rho_L - rho_R) * (rho_L - rho_R) + (u_L - u_R) * (u_L - u_R) + (p_L - p_R) * (p_L - p_R);
+        R scale = rho_L + rho_R + p_L + p_R + M<R>::abs_(u_L) + M<R>::abs_(u_R);
+        if constexpr (RS == 1) {
+            d2 = d2 + (L.v - Rr.v) * (L.v - Rr.v);
+            scale = scale + M<R>::abs_(L.v) + M<R>::abs_(Rr.v);
+        }
+        const R th = StarPolicy<R>::threshold(scale, G);
+        return d2 < th * th;
     }
 }
 
