@@ -52,6 +52,8 @@ struct BatchDev {
     const int* tile_local;        // [ntiles] tile index within its problem (y-tiles fastest)
     const int* order;             // [ntiles] processing order of the flat tiles
     const int* tiles_y;           // [nprob] tiles along y (the contiguous axis)
+    const int4* rec;              // [ntiles] per processing position k: problem, tile within it,
+                                  // tiles along y of the problem (one load per tile)
     int ntiles, nprob, steps, dynamic, stats;
     unsigned int* work;           // [2] per-step work counters (dynamic schedules)
     unsigned int* bar_count;      // grid barrier: arrivals
@@ -110,10 +112,13 @@ __device__ __forceinline__ bool grid_barrier(const BatchDev& B)
 // thread makes the halting decision from the same control block (the keys it
 // reads were final at the previous step's barrier, so all agree), and the
 // block copies the arguments word by word: one barrier per tile.
-__device__ __forceinline__ bool batch_tile_args(const BatchDev& B, int t, int step, StepArgs<float>& sa, int& lt)
+__device__ __forceinline__ bool batch_tile_args(const BatchDev& B, int k, int step, StepArgs<float>& sa, int& lt,
+                                                int& nty)
 {
-    const int p = B.tile_prob[t];
-    lt = B.tile_local[t];
+    const int4 r = B.rec[k];
+    const int p = r.x;
+    lt = r.y;
+    nty = r.z;
     volatile Ctl* c = B.ctl + p;
     bool ok = c->halted_seq == 0;
     if (ok && step > 1) {
@@ -145,15 +150,14 @@ __device__ __forceinline__ bool batch_tile_args(const BatchDev& B, int t, int st
     return ok;
 }
 
+// The tile at processing position k.
 template <int TJ, int TI, int NT>
-__device__ __forceinline__ void batch_tile(const BatchDev& B, int t, int step, StepArgs<float>& sa, unsigned char* smem,
+__device__ __forceinline__ void batch_tile(const BatchDev& B, int k, int step, StepArgs<float>& sa, unsigned char* smem,
                                            const MlpShared& M, bool last_tile = false)
 {
-    int lt;
-    if (batch_tile_args(B, t, step, sa, lt)) {
-        const int nty = B.tiles_y[B.tile_prob[t]];
+    int lt, nty;
+    if (batch_tile_args(B, k, step, sa, lt, nty))
         unsplit_tile<float, TJ, TI, NT, false>(sa, B.G, (lt % nty) * TI, (lt / nty) * TJ, smem, M, last_tile);
-    }
 }
 
 // ONE cooperative kernel for all steps of all problems.  The schedule only
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_persistent(const __grid_cons
             return r;
         };
         for (int k = B.dynamic ? next(0) : (int)blockIdx.x; k < B.ntiles; k = next(k))
-            batch_tile<TJ, TI, NT>(B, B.order[k], step, sa, smem_raw, M);
+            batch_tile<TJ, TI, NT>(B, k, step, sa, smem_raw, M);
         // the counter of the next step was last used two steps ago: reset it
         if (B.dynamic && blockIdx.x == 0 && threadIdx.x == 0)
             B.work[(step + 1) & 1] = 0u;
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_step(const __grid_constant__
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ StepArgs<float> sa;
     const MlpShared& M = *reinterpret_cast<const MlpShared*>(smem_raw);
-    batch_tile<TJ, TI, NT>(B, B.order[blockIdx.x], step, sa, smem_raw, M, true);
+    batch_tile<TJ, TI, NT>(B, blockIdx.x, step, sa, smem_raw, M, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -435,6 +439,8 @@ struct hydro_batch {
     StepArgs<float>* args = nullptr;
     int* tables = nullptr;
     size_t tables_cap = 0;
+    int4* rec = nullptr;
+    size_t rec_cap = 0;
     unsigned int* sync = nullptr;  // work[2], bar_count, bar_gen, bar_err
     double* stage = nullptr;
     unsigned long long* red = nullptr;
@@ -464,6 +470,7 @@ struct hydro_batch {
         cudaFree(ctl);
         cudaFree(args);
         cudaFree(tables);
+        cudaFree(rec);
         cudaFree(sync);
         cudaFree(stage);
         cudaFree(red);
@@ -617,6 +624,21 @@ static int batch_prepare(hydro_batch* b, const double* cfg, int ncfg, int steps,
     cudaMemcpyAsync(b->tables + nt, tlocal.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, b->stream);
     cudaMemcpyAsync(b->tables + 2 * (size_t)nt, order.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, b->stream);
     cudaMemcpyAsync(b->tables + 3 * (size_t)nt, ty.data(), sizeof(int) * np, cudaMemcpyHostToDevice, b->stream);
+    // per processing position: the tile's problem, its index there, the problem's tiles along y
+    std::vector<int4> rec(nt);
+    for (int k = 0; k < nt; ++k) {
+        const int t = order[k];
+        rec[k] = make_int4(tprob[t], tlocal[t], ty[tprob[t]], 0);
+    }
+    if ((size_t)nt > b->rec_cap) {
+        cudaFree(b->rec);
+        b->rec = nullptr;
+        b->rec_cap = 0;
+        if (!cuda_ok(cudaMalloc(&b->rec, sizeof(int4) * nt), "batch tile records"))
+            return -1;
+        b->rec_cap = nt;
+    }
+    cudaMemcpyAsync(b->rec, rec.data(), sizeof(int4) * nt, cudaMemcpyHostToDevice, b->stream);
     cudaMemcpyAsync(b->args, args.data(), sizeof(StepArgs<float>) * BATCH_VERSIONS * np, cudaMemcpyHostToDevice,
                     b->stream);
     *ntiles = nt;
@@ -885,6 +907,7 @@ int hydro_batch_run(hydro_batch* b, const double* cfg, int ncfg, int steps, int 
     B.tile_local = b->tables + nt;
     B.order = b->tables + 2 * (size_t)nt;
     B.tiles_y = b->tables + 3 * (size_t)nt;
+    B.rec = b->rec;
     B.ntiles = nt;
     B.nprob = b->nprob;
     B.steps = steps;
