@@ -106,47 +106,54 @@ __device__ __forceinline__ bool grid_barrier(const BatchDev& B)
     return *((volatile int*)B.bar_err) == 0;
 }
 
-// Loads the step arguments of flat tile t into shared memory and applies the
-// one-problem kernel's halting protocol (halt_prologue) per problem.  Returns
-// false (uniformly over the block) when the tile's problem has halted.  Every
-// thread makes the halting decision from the same control block (the keys it
-// reads were final at the previous step's barrier, so all agree), and the
-// block copies the arguments word by word: one barrier per tile.
+// Loads the step arguments of the tile at processing position k into shared
+// memory and applies the one-problem kernel's halting protocol (halt_prologue)
+// for its problem.  Returns false (uniformly over the block) when the problem
+// has halted.  One thread reads the control block and decides; the block
+// copies the arguments word by word meanwhile (also for a halted problem: its
+// arguments exist, and the copy is not used) and one barrier publishes both.
 __device__ __forceinline__ bool batch_tile_args(const BatchDev& B, int k, int step, StepArgs<float>& sa, int& lt,
                                                 int& nty)
 {
+    __shared__ int s_ok;
     const int4 r = B.rec[k];
     const int p = r.x;
     lt = r.y;
     nty = r.z;
-    volatile Ctl* c = B.ctl + p;
-    bool ok = c->halted_seq == 0;
-    if (ok && step > 1) {
-        const int ps = (step - 1) % 3;
-        const int d = halt_decision(c->key[ps][0], c->key[ps][1], c->upd_bad[ps]);
-        if (d) {
-            ok = false;
-            if (lt == 0 && threadIdx.x == 0) {
-                c->halt_kind = d;
-                c->halted_seq = step - 1;
+    if (threadIdx.x == 0) {
+        volatile Ctl* c = B.ctl + p;
+        bool ok = c->halted_seq == 0;
+        if (ok && step > 1) {
+            const int ps = (step - 1) % 3;
+            const int d = halt_decision(c->key[ps][0], c->key[ps][1], c->upd_bad[ps]);
+            if (d) {
+                ok = false;
+                if (lt == 0) {
+                    c->halt_kind = d;
+                    c->halted_seq = step - 1;
+                }
             }
         }
-    }
-    if (ok) {
-        if (lt == 0 && threadIdx.x == 0) {
+        if (ok && lt == 0) {
             const int ns = (step + 1) % 3;
             c->key[ns][0] = 0ull;
             c->key[ns][1] = 0ull;
             c->upd_bad[ns] = 0u;
         }
-        constexpr int WORDS = (int)(sizeof(StepArgs<float>) / 4);
-        static_assert(sizeof(StepArgs<float>) % 4 == 0, "word copy");
-        const int* src = reinterpret_cast<const int*>(B.args + (size_t)p * BATCH_VERSIONS + batch_version(step));
-        int* dst = reinterpret_cast<int*>(&sa);
-        for (int w = threadIdx.x; w < WORDS; w += blockDim.x)
-            dst[w] = src[w];
+        s_ok = ok ? 1 : 0;
     }
+    constexpr int WORDS = (int)(sizeof(StepArgs<float>) / 4);
+    static_assert(sizeof(StepArgs<float>) % 4 == 0, "word copy");
+    const int* src = reinterpret_cast<const int*>(B.args + (size_t)p * BATCH_VERSIONS + batch_version(step));
+    int* dst = reinterpret_cast<int*>(&sa);
+    for (int w = threadIdx.x; w < WORDS; w += blockDim.x)
+        dst[w] = src[w];
     __syncthreads();
+    const bool ok = s_ok != 0;
+    // a skipped tile: every thread has read s_ok before the next tile's decision
+    // overwrites it (a computed tile's own barriers do this)
+    if (!ok)
+        __syncthreads();
     return ok;
 }
 
