@@ -11,8 +11,10 @@ value       FP32 form with the learned Newton starting pressure (the headline
             larger than L2, so no flush is needed between steps).
 e2e         the same form through the reference's scheme call
             GRP_solver_2D_EUL_source (config[300] = 2) from host arrays:
-            upload, K steps, download and the call's own set-up inside the
-            timed region (wall clock around the call).
+            upload, K steps and download inside the timed region (wall clock
+            around the call; the second call on the same host arrays, which
+            reuses the solver the entry point kept from the first; the first
+            call is reported beside it).
 forms       plain FP32 and the FP64 parity form on the same grid and steps,
             relative L1 of every FP32 result against the FP64 result, FP64
             conservation integrals, Newton statistics.
@@ -20,8 +22,9 @@ roofline    HBM roofline of the step kernel: 96 algorithmic bytes per FP32
             cell-update (the carried state, 4 primitives + 8 limiter slopes,
             read once and written once; 192 B in FP64).
 batch       512 independent four-quadrant problems, N x N with N uniform in
-            {64, 96, ..., 512}, 300 steps, one persistent kernel under a CUDA
-            graph with the autotuned tile shape and schedule.
+            {64, 96, ..., 512}, 300 steps, captured in a CUDA graph with the
+            autotuned tile shape and schedule (one persistent kernel, or one
+            launch per step).
 cpu_baseline the oracle's C restatement of the reference's CPU path (OpenMP,
             all host cores) on a bounded number of steps of the same grid.
 
