@@ -682,13 +682,19 @@ __device__ __forceinline__ void q1d_waves(const Side<R>& L, const Side<R>& Rr, c
 // only a few percent of the faces of piecewise-smooth data get here, and
 // keeping it separate leaves the common (uniform-pair) path its registers.
 template <typename R, bool FUSED = true>
-__device__ __noinline__ void q1d_star_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
-                                            StarInfo& st, R p_start)
+__device__ __forceinline__ void q1d_star_exact_body(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
+                                                    StarInfo& st, R p_start)
 {
     StarPolicy<R>::template solve<FUSED>(L.u, Rr.u, L.p, Rr.p, S.c_L, S.c_R, G, p_start, S.u_star, S.p_star, st);
     S.crw0 = st.crw0;
     S.crw1 = st.crw1;
     q1d_waves(L, Rr, G, S);
+}
+template <typename R, bool FUSED = true>
+__device__ __noinline__ void q1d_star_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, Star<R>& S,
+                                            StarInfo& st, R p_start)
+{
+    q1d_star_exact_body<R, FUSED>(L, Rr, G, S, st, p_start);
 }
 
 // Star state of linear_GRP_solver_Edir_Q1D (:92-134) with atc = eps:
@@ -754,7 +760,14 @@ __device__ __forceinline__ void q1d_star(const Side<R>& L, const Side<R>& Rr, co
         return;
     }
     if constexpr (KNOWN != 1)  // no out-of-line call (and its addressed arguments) on the uniform path
-        q1d_star_exact<R, FUSED>(L, Rr, G, S, st, p_start);
+    {
+        // FP32: the exact path inline (no call, no arguments through the stack);
+        // FP64: out of line, as its register footprint would burden the common path
+        if constexpr (sizeof(R) == 4)
+            q1d_star_exact_body<R, FUSED>(L, Rr, G, S, st, p_start);
+        else
+            q1d_star_exact<R, FUSED>(L, Rr, G, S, st, p_start);
+    }
 }
 
 // Waves of the star state (linear_grp_solver_Edir_Q1D.c:110-133).
@@ -788,6 +801,9 @@ __device__ __forceinline__ void q1d_waves(const Side<R>& L, const Side<R>& Rr, c
 template <typename R>
 __device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
                                               R D[4], R U[4]);
+template <typename R>
+__device__ __forceinline__ void q1d_derivs_exact_body(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G,
+                                                      const Star<R>& S, R D[4], R U[4]);
 
 template <typename R>
 __device__ __noinline__ void g2d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G,
@@ -865,6 +881,8 @@ __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, 
     if constexpr (KNOWN != 1) {
         if constexpr (RS == 1)
             g2d_derivs_exact(L, Rr, G, S, D, U);
+        else if constexpr (sizeof(R) == 4)
+            q1d_derivs_exact_body<R>(L, Rr, G, S, D, U);
         else
             q1d_derivs_exact(L, Rr, G, S, D, U);
     }
@@ -872,8 +890,8 @@ __device__ __forceinline__ void q1d_derivs(const Side<R>& L, const Side<R>& Rr, 
 
 // Non-acoustic case of the quasi-1D GRP (:256-547), out of line like q1d_star_exact.
 template <typename R>
-__device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
-                                              R D[4], R U[4])
+__device__ __forceinline__ void q1d_derivs_exact_body(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G,
+                                                      const Star<R>& S, R D[4], R U[4])
 {
     const R rho_L = L.rho, rho_R = Rr.rho;
     const R d_rho_L = L.drho, d_rho_R = Rr.drho, t_rho_L = L.trho, t_rho_R = Rr.trho;
@@ -1069,6 +1087,12 @@ __device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& R
         D[2] = D[2] - U[2] * t_v_R - T_p / U[0];
         D[3] = D[3] - U[2] * T_p - U[0] * C * C * t_v_R;
     }
+}
+template <typename R>
+__device__ __noinline__ void q1d_derivs_exact(const Side<R>& L, const Side<R>& Rr, const Gas<R>& G, const Star<R>& S,
+                                              R D[4], R U[4])
+{
+    q1d_derivs_exact_body<R>(L, Rr, G, S, D, U);
 }
 
 // Interface result: mid-time flux (F_rho, F_u, F_v, F_e) in the x/y frame and
