@@ -39,22 +39,30 @@ bool cuda_ok(cudaError_t e, const char* what)
     return false;
 }
 
-bool pageable_host_access()
+int host_rows_mode()
 {
-    // measured on GB300 + Grace: a 4096^2 state moves faster staged (host
-    // gather + one copy per field) than read row by row by the GPU, so the
-    // direct path is opt-in
+    // measured on GB300 + Grace, 4096^2, 20 steps, the second call on the same
+    // host arrays: 24.9-25.1 ms staged both ways, 22.8 ms with the upload
+    // direct, 21.9 ms direct both ways; but a direct download into rows the
+    // host never touched takes their page faults on the GPU (0.19 s for such
+    // a first call, against 27-44 ms with the download staged).  So by
+    // default the GPU reads the caller's rows (already written by the caller)
+    // and the download stays staged.
     const char* e = getenv("HYDRO_DIRECT_HOST_ROWS");
-    if (!e || atoi(e) == 0)
-        return false;
-    int dev = 0, v = 0;
+    const int want = !e ? 1 : strcmp(e, "in") == 0 ? 1 : atoi(e) != 0 ? 3 : 0;
+    if (!want)
+        return 0;
+    int dev = 0, v = 0, ats = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)
-        return false;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+        return 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
-    return v == 1;
+    // the default only where the GPU walks the host's own page tables
+    // (address translation services); on request wherever access is coherent
+    return v == 1 && (e || ats == 1) ? want : 0;
 }
 
 RunConfig run_config_from(const double* cfg, int ncfg)
@@ -392,9 +400,9 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
     // reads pageable host memory coherently (Grace-Blackwell), the kernels
     // gather and scatter those rows themselves; elsewhere the rows are packed
     // into one host buffer and copied.
-    const bool direct = pageable_host_access();
+    const int direct = host_rows_mode();
     const double* const* in_rows[5] = {CV[0].RHO, CV[0].U, CV[0].V, CV[0].P, CV[0].E};
-    if (direct ? s->upload_rows(in_rows) : s->upload_rows_staged(in_rows)) {
+    if ((direct & 1) ? s->upload_rows(in_rows) : s->upload_rows_staged(in_rows)) {
         fprintf(stderr, "hydro_gb300: upload failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }
@@ -412,7 +420,7 @@ static void run_2d_entry(const int m, const int n, struct cell_var_stru* CV, dou
         exit(5);
     }
     double* const* out_rows[5] = {CV[nt].RHO, CV[nt].U, CV[nt].V, CV[nt].P, CV[nt].E};
-    if (direct ? s->download_rows(out_rows) : s->download_rows_staged(out_rows)) {
+    if ((direct & 2) ? s->download_rows(out_rows) : s->download_rows_staged(out_rows)) {
         fprintf(stderr, "hydro_gb300: download failed: %s\n", hydro_gb300_last_error());
         exit(5);
     }

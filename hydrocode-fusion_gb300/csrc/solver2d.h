@@ -60,7 +60,7 @@ public:
     virtual int download(double* rho, double* u, double* v, double* p, double* E) = 0;
     // The same from/to the caller's row arrays (rows[k][j] = row j of field k:
     // rho, u, v, p, E), read and written by the GPU itself; only where the
-    // device accesses pageable host memory coherently (pageable_host_access()).
+    // device accesses pageable host memory coherently (host_rows_mode()).
     virtual int upload_rows(const double* const* const rows[5]) = 0;
     virtual int download_rows(double* const* const rows[5]) = 0;
     // The same through the host staging pair (host_pair()): host threads pack
@@ -87,10 +87,13 @@ public:
 Solver2DBase* make_solver2d_f64(int m, int n, int rs);
 Solver2DBase* make_solver2d_f32(int m, int n, int learned, int rs);
 
-// True when HYDRO_DIRECT_HOST_ROWS=1 asks for it and the current device reads
-// and writes pageable host memory coherently (Grace-Blackwell address
-// translation), so kernels may take the caller's malloc'd rows directly.
-bool pageable_host_access();
+// Which of the scheme entry points' row copies the GPU makes itself, reading
+// or writing the caller's malloc'd rows (Grace-Blackwell address translation):
+// bit 0 the upload, bit 1 the download; 0 where the current device does not
+// access pageable host memory coherently.  HYDRO_DIRECT_HOST_ROWS picks it:
+// 0 none, 1 both, "in" the upload only; unset, the upload only where the
+// GPU walks the host's page tables (address translation services), else none.
+int host_rows_mode();
 
 // Two host buffers for the scheme entry points' row copies, pinned where the
 // driver grants it (else ordinary memory), kept for the life of the process;

@@ -28,14 +28,17 @@ def test_2d_entry_with_plot_snapshots(gpu_lib, host_path):
             assert rel_l1(data[k, f], snaps[k, f]) <= TOL, (k, f)
 
 
-@pytest.fixture(params=["direct", "staged"])
+@pytest.fixture(params=["direct", "default", "staged"])
 def host_path(request, monkeypatch):
-    """Both ways the scheme call moves the caller's rows: packed into one host
-    buffer and copied (the default), and read and written by the GPU itself
-    (HYDRO_DIRECT_HOST_ROWS=1, where it accesses pageable host memory
-    coherently)."""
+    """The ways the scheme call moves the caller's rows: read and written by
+    the GPU itself (HYDRO_DIRECT_HOST_ROWS=1, where it accesses pageable host
+    memory coherently), the default (read by the GPU where it walks the host's
+    page tables, written back staged), and packed into one host buffer and
+    copied both ways (HYDRO_DIRECT_HOST_ROWS=0)."""
     if request.param == "direct":
         monkeypatch.setenv("HYDRO_DIRECT_HOST_ROWS", "1")
+    elif request.param == "staged":
+        monkeypatch.setenv("HYDRO_DIRECT_HOST_ROWS", "0")
     else:
         monkeypatch.delenv("HYDRO_DIRECT_HOST_ROWS", raising=False)
     return request.param
@@ -72,13 +75,15 @@ def test_1d_entry_sod(gpu_lib, order):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("rows", ["0", "in"])
 @pytest.mark.parametrize("form", [0, 1, 2])
-def test_entry_row_copies_match_plane_api(gpu_lib, form, monkeypatch):
-    """The scheme call's staged row copies (host threads pack the caller's
+def test_entry_row_copies_match_plane_api(gpu_lib, form, rows, monkeypatch):
+    """The scheme call's row copies, staged (host threads pack the caller's
     rows, converted to the form's precision, through a pair of host buffers)
-    and the plane API (the device converts) leave the same state bit for bit,
-    values at and below the float subnormal range included."""
-    monkeypatch.delenv("HYDRO_DIRECT_HOST_ROWS", raising=False)
+    or read by the GPU itself, and the plane API (the device converts) leave
+    the same state bit for bit, values at and below the float subnormal range
+    included."""
+    monkeypatch.setenv("HYDRO_DIRECT_HOST_ROWS", rows)
     hg = gpu_lib
     from hydro_gb300 import cases
 
