@@ -331,7 +331,7 @@ __device__ __forceinline__ void batch_strip_unit(const BatchStripDev& D, int e, 
     const int r0 = seg * SEG;
     unsigned bad = 0;
     strip_unit<false>(a, &B.G, strip * STRIP_W, r0, (r0 + SEG < a.m) ? r0 + SEG : a.m, q, nullptr, STRIP_MLP_MIN,
-                      stats3, bad);
+                      LEARNED_JUMP2_MIN, stats3, bad);
     strip_report(a.ctl, step % 3, B.stats, stats3, bad);
 }
 

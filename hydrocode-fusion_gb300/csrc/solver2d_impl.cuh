@@ -253,6 +253,18 @@ __global__ void k_cfl_min(const R* __restrict__ w, size_t plane, int m, int n, i
 }
 
 // True when h is a power of two (then d/h == d*(1/h) exactly).
+// The strip kernel's strong-jump threshold of the learned start
+// (LEARNED_JUMP2_MIN unless HYDRO_LEARNED_JUMP2 gives another), read once.
+inline float learned_jump2()
+{
+    static const float v = [] {
+        const char* e = getenv("HYDRO_LEARNED_JUMP2");
+        const float x = e ? (float)atof(e) : LEARNED_JUMP2_MIN;
+        return x >= 0.f ? x : LEARNED_JUMP2_MIN;
+    }();
+    return v;
+}
+
 inline bool h_is_pow2(double h)
 {
     int e;
@@ -945,6 +957,7 @@ public:
                     sa.work = work;
                     sa.seg = V.TJ;
                     sa.mlp_min = V.mlp_min;
+                    sa.mlp_jump2 = learned_jump2();
                     sa.mlp_global = V.mlp_global;
                     void* args[] = {(void*)&a, (void*)&sa};
                     // variants of one kernel differ in their L1/shared split: set per launch

@@ -289,12 +289,28 @@ constexpr float LEARNED_JUMP2_MIN = 0.005f;
 // speeds taken, when no lane needs it).  Returns -1 where no guess applies
 // (weak jump, inactive lane, a pair that would generate vacuum, a non-finite
 // prediction).
+__device__ __forceinline__ bool learned_strong_jump(float rhoL, float uL, float pL, float rhoR, float uR, float pR,
+                                                   float g, float jump2)
+{
+    const float sp = pL + pR, dp = pL - pR, du = uL - uR;
+    const float w = g * (pL * rhoR + pR * rhoL);  // gamma (pL/rhoL + pR/rhoR) rhoL rhoR
+    return dp * dp * w + du * du * (rhoL * rhoR) * (sp * sp) >= jump2 * (sp * sp) * w;
+}
+
+// The network's start for the lanes with need set (warp-collective, as below).
+__device__ __forceinline__ float learned_start(const Side<float>& L, const Side<float>& Rr, bool need,
+                                               const Gas<float>& G, const MlpShared& M, int rows);
+
 __device__ __forceinline__ float learned_guess(const Side<float>& L, const Side<float>& Rr, bool active,
                                                const Gas<float>& G, const MlpShared& M, int rows)
 {
-    const float sp = L.p + Rr.p, dp = L.p - Rr.p, du = L.u - Rr.u;
-    const float w = G.g * (L.p * Rr.rho + Rr.p * L.rho);  // gamma (pL/rhoL + pR/rhoR) rhoL rhoR
-    const bool need = active && dp * dp * w + du * du * (L.rho * Rr.rho) * (sp * sp) >= LEARNED_JUMP2_MIN * (sp * sp) * w;
+    const bool need = active && learned_strong_jump(L.rho, L.u, L.p, Rr.rho, Rr.u, Rr.p, G.g, LEARNED_JUMP2_MIN);
+    return learned_start(L, Rr, need, G, M, rows);
+}
+
+__device__ __forceinline__ float learned_start(const Side<float>& L, const Side<float>& Rr, bool need,
+                                               const Gas<float>& G, const MlpShared& M, int rows)
+{
     float pg = -1.f;
     if (__any_sync(0xffffffffu, need)) {
         const float cL = sqrtf(G.g * L.p / L.rho), cR = sqrtf(G.g * Rr.p / Rr.rho);

@@ -319,7 +319,8 @@ __device__ __forceinline__ void strip_face_pair(const SSide2& L, const SSide2& R
 // ---------------------------------------------------------------------------
 // entry: L[12] R[12] (Side<float> order), row, col, flags (bit 0 dir (1 = y-face),
 // bit 1 mode (1 = FP64 retry of an acoustic face), bit 2 counted in the
-// statistics); after the flush, words 0..7 hold the outputs F[4] I[4] in the
+// statistics), the learned starting pressure (word 27, learned form); after
+// the flush, words 0..7 hold the outputs F[4] I[4] in the
 // strip's normal-frame convention.
 __device__ __forceinline__ void strip_put_side(float* e, const SSide2& S, bool y)
 {
@@ -337,6 +338,7 @@ struct StripFlushArgs {
     float tau, htau;
     int m, n, slot;
     int mlp_min;  // learned form: the network runs on flushes of at least this many faces
+    float mlp_jump2;  // learned form: the strong-jump threshold of learned_guess
 };
 
 template <bool LEARNED>
@@ -359,7 +361,9 @@ static __device__ __noinline__ void strip_flush(float* q, int cnt, const StripFl
             L.rho = e[0]; L.u = e[1]; L.v = e[2]; L.p = e[3];
             Rr.rho = e[12]; Rr.u = e[13]; Rr.v = e[14]; Rr.p = e[15];
             const bool retry = (__float_as_int(e[26]) >> 1) & 1;
-            const float ps = learned_guess(L, Rr, act && !retry, G, *M, cnt - base < 32 ? cnt - base : 32);
+            const bool need = act && !retry &&
+                              learned_strong_jump(L.rho, L.u, L.p, Rr.rho, Rr.u, Rr.p, G.g, fa.mlp_jump2);
+            const float ps = learned_start(L, Rr, need, G, *M, cnt - base < 32 ? cnt - base : 32);
             if (act)
                 e[27] = ps;
         }
@@ -481,6 +485,7 @@ struct StripArgs {
     unsigned int* work;  // three rotating per-launch unit counters
     int seg;             // rows per work unit
     int mlp_min;         // learned form: smallest queue flush the network runs on
+    float mlp_jump2;     // learned form: the strong-jump threshold of learned_guess
     int mlp_global;      // learned form: 1 = read the network image from global memory (through L1)
 };
 
@@ -499,13 +504,14 @@ struct StripSmem {
 // strip_report).
 template <bool LEARNED, class A>
 __device__ __forceinline__ void strip_unit(const A& a, const Gas<float>* Gp, int c0, int r0, int r1, float* q,
-                                           const MlpShared* M, int mlp_min, int* stats3, unsigned& bad)
+                                           const MlpShared* M, int mlp_min, float mlp_jump2, int* stats3,
+                                           unsigned& bad)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int m = a.m, n = a.n, slot = a.seq % 3;
     const Gas<float>& G = *Gp;
-    const StripFlushArgs fa{Gp, a.ctl, a.tau, a.htau, m, n, slot, mlp_min};
+    const StripFlushArgs fa{Gp, a.ctl, a.tau, a.htau, m, n, slot, mlp_min, mlp_jump2};
     const float ihx = a.pow2_x ? a.inv_hx : 1.f / a.hx, ihy = a.pow2_y ? a.inv_hy : 1.f / a.hy;
     const float ahx = a.alpha * ihx, ahy = a.alpha * ihy;
     const float hhx = a.hhx, hhy = a.hhy;
@@ -796,7 +802,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) k_step_strip(const __grid_const
         const int seg = u / nstrip, strip = u - seg * nstrip;
         const int r0 = seg * sa.seg;
         strip_unit<LEARNED>(a, &a.G, strip * STRIP_W, r0, (r0 + sa.seg < a.m) ? r0 + sa.seg : a.m, q, M, sa.mlp_min,
-                            stats3, bad);
+                            sa.mlp_jump2, stats3, bad);
     }
     strip_report(a.ctl, a.seq % 3, a.stats, stats3, bad);
 }
